@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""Throughput of the FVDBM step (MCUPS and fraction of the HBM roofline).
+
+Workload (default): the porous square, 400 seeded circular obstacles at
+porosity 0.70, ~1M triangles, D2Q9, tau=0.6, dt=0.5*min edge, upwind,
+inlet rho=1.001 / outlet rho=1.0 density nodes, no-slip walls and obstacles,
+float32.  Inputs are synthetic (seeded mesh generator; Triangle is not
+available).
+
+A bench step is one FVDBM time step over the whole mesh.  Between timed steps
+L2 is flushed by writing a buffer of 2x L2 size on the step's stream, so each
+timed step reads its inputs from HBM.  Each step is bracketed by CUDA events
+on the library's stream; the cell kernel (the dominant one) is timed on its
+own for the roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N>1) every rank runs an independent replica (a differently
+seeded mesh of the same size): units processed over all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "MCUPS at 1M tris (% HBM roofline); time-to-steady @1e-6 resid, warm vs plain"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=200)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="porous1m", choices=["porous1m", "cavity", "channel"])
+    ap.add_argument("--flux", default="upwind", choices=["upwind", "lax_wendroff"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    return ap.parse_args()
+
+
+def workload(name, flux, seed):
+    from fvdbm_jax_gb300 import D2Q9, Mesher, meshgen
+    t0 = time.perf_counter()
+    if name == "porous1m":
+        raw = meshgen.porous(n_obstacles=400, n_target=1_000_000, porosity=0.70, seed=seed)
+        tau = 0.6
+    elif name == "channel":
+        raw = meshgen.channel_cylinder(seed=seed)
+        tau = 0.55
+    else:
+        raw = meshgen.cavity(seed=seed)
+        tau = 0.6
+    m = Mesher().import_meshpy(raw)
+    m.calc_mesh_properties()
+    dyn = D2Q9(tau, 0.5 * float(m.face_lengths.min()))
+    c, f, n = m.to_env(dyn, flux)
+    if name == "porous1m":
+        for mk in (1, 3, 5):
+            n = m.set_vel_node(n, mk, (0.0, 0.0))
+        n = m.set_rho_node(n, 4, 1.001)
+        n = m.set_rho_node(n, 2, 1.0)
+    elif name == "channel":
+        import numpy as np
+        for mk in (1, 3, 5):
+            n = m.set_vel_node(n, mk, (0.0, 0.0))
+        n = m.set_vel_node(n, 4, (0.0, 0.0))
+        sel = m.point_markers == 4
+        y = m.points[sel, 1]
+        v = np.array(n.vel)
+        v[sel, 0] = 4 * 0.1 * y * (0.41 - y) / 0.41 ** 2
+        n.vel = v
+        n = m.set_rho_node(n, 2, 1.0)
+    else:
+        for mk in (1, 2, 4):
+            n = m.set_vel_node(n, mk, (0.0, 0.0))
+        n = m.set_vel_node(n, 3, (0.1, 0.0))
+    desc = {"workload": {"porous1m": "porous square, 400 obstacles, ~1M triangles",
+                         "channel": "channel 2.2x0.41 with cylinder, ~60k triangles",
+                         "cavity": "lid-driven cavity 41x41 grid, 3,200 triangles"}[name],
+            "cells": int(c.pdf.shape[0]), "faces": int(f.pdf.shape[0]), "nodes": int(n.pdf.shape[0]),
+            "lattice": "D2Q9", "flux": flux, "tau": tau, "delta_t": float(dyn.delta_t),
+            "porosity": float(raw.info.get("porosity", 1.0)) if name == "porous1m" else None,
+            "seed": seed, "setup_s": round(time.perf_counter() - t0, 2)}
+    return m, dyn, c, f, n, desc
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_key):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
+            return json.load(fh).get(kernel_key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def max_over_ranks(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_oracle_rate(c, f, n, dyn, seconds, threads=0):
+    """C restatement of the step on the host cores: MCUPS over a bounded
+    sample (whole steps of the same mesh until ``seconds`` elapse)."""
+    import oracle_c as OC
+    import oracle_np as O
+    geo = O.geo_from_containers(c, f, n)
+    st = O.state_from_containers(c, n)
+    pr = OC.Prepared(geo, dyn.inv_tau, dyn.dt32)
+    threads = threads or OC.max_threads()
+    OC.step(geo, st, dyn.inv_tau, dyn.dt32, n_steps=1, threads=threads, prepared=pr)  # warm
+    done, t0 = 0, time.perf_counter()
+    while True:
+        st = OC.step(geo, st, dyn.inv_tau, dyn.dt32, n_steps=1, threads=threads, prepared=pr)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or done >= 10_000:
+            break
+    N = int(c.pdf.shape[0])
+    return N * done / el / 1e6, threads, done, el
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup()
+    if rank != 0:
+        return
+    m, dyn, c, f, n, desc = workload(args.workload, args.flux, seed=0)
+    budget = max(5.0, min(150.0, 0.05 * args.steps + 10.0))
+    rate, threads, done, el = cpu_oracle_rate(c, f, n, dyn, budget)
+    N = int(c.pdf.shape[0])
+    line = {"impl": "reference", "metric": METRIC, "value": round(rate, 3), "unit": "MCUPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(el / done * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": desc,
+            "cpu_baseline": {"value": round(rate, 3), "unit": "MCUPS", "cores": threads, "kind": "port",
+                             "sample": f"{done} whole steps of the {N}-cell mesh ({el:.1f}s), "
+                                       f"C restatement of the reference step, OpenMP"},
+            "e2e": {"value": round(rate, 3), "unit": "MCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    from fvdbm_jax_gb300 import Environment
+    from fvdbm_jax_gb300 import _native as nat
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    m, dyn, c, f, n, desc = workload(args.workload, args.flux, seed=rank)
+    env = Environment(c, f, n, device=local)
+    env.init()
+    info = env.info()
+    L = nat.lib()
+    h = env.handle
+    N = info["n_cells"]
+    stream = torch.cuda.ExternalStream(env.stream_ptr, device=f"cuda:{local}")
+    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    # warm-up (graph replay, as a long run would)
+    env.step(max(args.warmup, 3))
+    env.sync()
+
+    K = args.steps
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    barrier(ws)
+    torch.cuda.synchronize(local)
+    env.sync()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    t_wall = time.perf_counter()
+    for k in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+        ev[k][0].record(stream)
+        nat.check(L.fvdbm_step_phase(h, 1), h)
+        ev[k][1].record(stream)
+        nat.check(L.fvdbm_step_phase(h, 2), h)
+        ev[k][2].record(stream)
+    env.sync()
+    torch.cuda.synchronize(local)
+    t_wall = time.perf_counter() - t_wall
+    barrier(ws)
+    clk = clocks.stop()
+    step_ms = [e[0].elapsed_time(e[2]) for e in ev]
+    node_ms = [e[0].elapsed_time(e[1]) for e in ev]
+    cell_ms = [e[1].elapsed_time(e[2]) for e in ev]
+    total_ms = sum(step_ms)
+    total_ms_max = max_over_ranks(total_ms, ws, local)
+    cells_all = sum_over_ranks(float(N), ws, local)
+    value = cells_all * K / (total_ms_max / 1e3) / 1e6
+
+    # the cell kernel's algorithmic bytes per launch: pdf read + write,
+    # cell->face slots, face geometry, ghost-node pdf read
+    F = info["n_faces"]
+    K3 = int(np.asarray(c.face_indices).shape[1])
+    cell_bytes = 72.0 * N + 4.0 * K3 * N + 20.0 * F + (8.0 * F if args.flux == "lax_wendroff" else 0.0) \
+        + 36.0 * info["n_bc_nodes"]
+    cell_avg_s = statistics.mean(cell_ms) / 1e3
+    peak, peak_kind = measured_peaks()
+    achieved = cell_bytes / cell_avg_s / 1e9
+    step_achieved = info["bytes_per_step"] / (statistics.mean(step_ms) / 1e3) / 1e9
+
+    # the same steps back to back from the captured CUDA graph, no flush (the
+    # state then partly stays in L2, as in a long run)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    resident_steps = 1024
+    env.step(64)
+    e0.record(stream)
+    env.step(resident_steps)
+    e1.record(stream)
+    env.sync()
+    res_ms = e0.elapsed_time(e1) / resident_steps
+
+    # end to end through the C ABI with host buffers: per step the pdf is
+    # copied in from pinned memory, one step runs, rho and vel are read back
+    pdf_h = torch.empty((N, 9), dtype=torch.float32, pin_memory=True).numpy()
+    rho_h = torch.empty((N,), dtype=torch.float32, pin_memory=True).numpy()
+    vel_h = torch.empty((N, 2), dtype=torch.float32, pin_memory=True).numpy()
+    nat.check(L.fvdbm_get_cells(h, nat.fptr(pdf_h), None, None, None), h)
+    E = max(3, min(args.e2e_steps, K))
+    for _ in range(2):
+        nat.check(L.fvdbm_set_state(h, nat.fptr(pdf_h), None, None, None), h)
+        nat.check(L.fvdbm_step(h, 1), h)
+        nat.check(L.fvdbm_get_cells(h, None, nat.fptr(rho_h), nat.fptr(vel_h), None), h)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(E):
+        nat.check(L.fvdbm_set_state(h, nat.fptr(pdf_h), None, None, None), h)
+        nat.check(L.fvdbm_step(h, 1), h)
+        nat.check(L.fvdbm_get_cells(h, None, nat.fptr(rho_h), nat.fptr(vel_h), None), h)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws, local)
+    e2e_value = cells_all * E / e2e_s / 1e6
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        rate, threads, done, el = cpu_oracle_rate(c, f, n, dyn, args.cpu_seconds)
+        cpu = {"value": round(rate, 3), "unit": "MCUPS", "cores": threads, "kind": "port",
+               "sample": f"{done} whole steps of the same {N}-cell mesh ({el:.1f}s), C restatement "
+                         f"of the reference step with OpenMP"}
+
+    if rank == 0:
+        desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                     "l2": "flushed between timed steps (2x L2 write on the step's stream)",
+                     "kernel": "fused" if info["kernel"] == 2 else "staged",
+                     "launches_per_step": info["launches_per_step"]})
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "MCUPS", "n_gpus": ws, "steps": K,
+            "warmup": args.warmup, "ms_per_step": round(total_ms_max / K, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": desc,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": profiled_traffic("cell_kernel"),
+                         "kernel": "k_fused" if info["kernel"] == 2 else "k_gather",
+                         "bytes_per_launch": cell_bytes, "avg_launch_us": round(cell_avg_s * 1e6, 3),
+                         "peak_kind": peak_kind,
+                         "step_frac": round(step_achieved / peak, 4),
+                         "node_kernel_avg_us": round(statistics.mean(node_ms) * 1e3, 3)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 3), "unit": "MCUPS", "h2d_bytes_per_step": 36 * N,
+                    "d2h_bytes_per_step": 12 * N, "steps": E},
+            "gpu_launches": K * info["launches_per_step"],
+            "clocks": clk,
+            "l2_resident": {"mcups": round(N / (res_ms / 1e3) / 1e6, 3), "ms_per_step": round(res_ms, 5),
+                            "steps": resident_steps, "note": "graph replay, no flush"},
+            "wall_s": round(t_wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    env.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

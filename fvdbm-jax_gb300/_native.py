@@ -1,0 +1,117 @@
+"""ctypes binding of libfvdbm.so (C ABI declared in include/fvdbm.h).
+
+Loading never falls back to anything: if the library is missing or cannot be
+loaded, ``lib()`` raises, so a GPU run can only ever go through the CUDA
+kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FVDBM_UPWIND, FVDBM_LAX_WENDROFF = 0, 1
+VARIANT_NONE, VARIANT_FACE_SCALE, VARIANT_FACE_Q_SCALE = 0, 1, 2
+ORDER_NONE, ORDER_RCM, ORDER_MORTON = 0, 1, 2
+KERNEL_AUTO, KERNEL_STAGED, KERNEL_FUSED = 0, 1, 2
+
+_i32p = C.POINTER(C.c_int32)
+_f32p = C.POINTER(C.c_float)
+
+
+class Mesh(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_nodes", C.c_int32),
+        ("cell_face_stride", C.c_int32), ("node_cell_stride", C.c_int32),
+        ("cell_face_indices", _i32p), ("cell_face_signs", _i32p),
+        ("face_cells", _i32p), ("face_dists", _f32p), ("face_nodes", _i32p),
+        ("face_n", _f32p), ("face_L", _f32p), ("face_scale", _f32p),
+        ("node_type", _i32p), ("node_cells", _i32p), ("node_dists", _f32p),
+        ("cell_xy", _f32p), ("cell_inv_area", _f32p),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("flux_scheme", C.c_int32), ("variant", C.c_int32),
+        ("inv_tau", C.c_float), ("delta_t", C.c_float),
+        ("c2", C.c_float), ("c4x2", C.c_float), ("c2x2", C.c_float),
+        ("ordering", C.c_int32), ("kernel", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_nodes", C.c_int32),
+        ("n_bc_nodes", C.c_int32), ("n_ghost_faces", C.c_int32), ("kernel", C.c_int32),
+        ("launches_per_step", C.c_int32), ("padded_cells", C.c_int32),
+        ("bytes_per_step", C.c_double), ("device_bytes", C.c_double),
+    ]
+
+
+_LIB = None
+EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", "fvdbm_get_cells", "fvdbm_get_nodes",
+           "fvdbm_get_face_fluxes", "fvdbm_sync", "fvdbm_stream", "fvdbm_get_info",
+           "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version"]
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True) -> C.CDLL:
+    """Load libfvdbm.so (building it first when the toolkit is present)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.build() if build_if_missing else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"libfvdbm.so not found at {path}; run __graft_entry__.build()")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.fvdbm_create.argtypes = [C.POINTER(Mesh), C.POINTER(Params), C.POINTER(vp)]
+    L.fvdbm_set_state.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]
+    L.fvdbm_step.argtypes = [vp, C.c_int32]
+    L.fvdbm_step_phase.argtypes = [vp, C.c_int32]
+    L.fvdbm_get_cells.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]
+    L.fvdbm_get_nodes.argtypes = [vp, _f32p, _f32p, _f32p]
+    L.fvdbm_get_face_fluxes.argtypes = [vp, _f32p]
+    L.fvdbm_sync.argtypes = [vp]
+    L.fvdbm_stream.argtypes = [vp]
+    L.fvdbm_stream.restype = vp
+    L.fvdbm_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.fvdbm_last_error.argtypes = [vp]
+    L.fvdbm_last_error.restype = C.c_char_p
+    L.fvdbm_destroy.argtypes = [vp]
+    L.fvdbm_abi_version.restype = C.c_int
+    for name in EXPORTS:
+        getattr(L, name)
+    if L.fvdbm_abi_version() != 1:
+        raise RuntimeError("libfvdbm ABI version mismatch")
+    _LIB = L
+    return L
+
+
+def fptr(a):
+    return None if a is None else a.ctypes.data_as(_f32p)
+
+
+def iptr(a):
+    return None if a is None else a.ctypes.data_as(_i32p)
+
+
+class FvdbmError(RuntimeError):
+    pass
+
+
+def check(rc: int, handle=None):
+    if rc != 0:
+        msg = lib().fvdbm_last_error(handle)
+        raise FvdbmError(f"libfvdbm error {rc}: {msg.decode() if msg else ''}")
+
+
+def c_contig(a, dtype):
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype)

@@ -1,0 +1,503 @@
+// C ABI of libfvdbm (declared in include/fvdbm.h).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fvdbm.h"
+#include "fvdbm_internal.h"
+
+namespace fvdbm {
+
+// [9][Np] device order -> [N][9] reference order.
+__global__ void k_soa_to_aos(const float* __restrict__ src, float* __restrict__ dst,
+                             const int* __restrict__ cell_new, int N, int Np, int rows) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int d = cell_new[c];
+  for (int q = 0; q < rows; ++q) dst[size_t(c) * rows + q] = src[size_t(q) * Np + d];
+}
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+constexpr int kGraphSteps = 32;  // steps per captured graph (even)
+
+struct Handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  HostPlan hp;
+  DevPlan dp{};
+  fvdbm_params_t params{};
+  std::vector<void*> allocs;
+  double device_bytes = 0;
+  float* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  float* flux = nullptr;
+  float* stage = nullptr;  // [N][9] staging (reference order)
+  int* d_cell_new = nullptr;
+  float* mac = nullptr;  // rho [Np], vel [2][Np], feq [9][Np]
+  long long steps_done = 0;
+  bool fused = false;
+  std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  std::string err;
+};
+
+int fail(Handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(h, FVDBM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(Handle* h, T** out, size_t n, const std::vector<T>* init = nullptr) {
+  *out = nullptr;
+  if (n == 0) n = 1;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(h, FVDBM_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  h->allocs.push_back(p);
+  h->device_bytes += double(n * sizeof(T));
+  *out = static_cast<T*>(p);
+  if (init && !init->empty()) {
+    e = cudaMemcpyAsync(p, init->data(), init->size() * sizeof(T), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return fail(h, FVDBM_ECUDA, std::string("upload: ") + cudaGetErrorString(e));
+  }
+  return FVDBM_OK;
+}
+
+#define DA(ptr, n, init)                                  \
+  do {                                                    \
+    int rc_ = dalloc(h, &(ptr), (n), (init));             \
+    if (rc_ != FVDBM_OK) return rc_;                      \
+  } while (0)
+
+int upload_nodes(Handle* h) {
+  const HostPlan& hp = h->hp;
+  if (hp.M == 0) return FVDBM_OK;
+  std::vector<float> pdf(size_t(Q) * hp.Mp, 0.0f), rho(hp.Mp, 0.0f), vel(size_t(2) * hp.Mp, 0.0f);
+  for (int d = 0; d < hp.M; ++d) {
+    const int p = hp.node_orig[d];
+    for (int q = 0; q < Q; ++q) pdf[size_t(q) * hp.Mp + d] = h->node_pdf[size_t(p) * Q + q];
+    rho[d] = h->node_rho[p];
+    vel[d] = h->node_vel[size_t(p) * 2];
+    vel[hp.Mp + d] = h->node_vel[size_t(p) * 2 + 1];
+  }
+  CK(cudaMemcpyAsync(h->dp.node_pdf, pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->dp.node_rho, rho.data(), rho.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->dp.node_vel, vel.data(), vel.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  // pageable sources: make sure the copies finished before the vectors die
+  CK(cudaStreamSynchronize(h->stream));
+  return FVDBM_OK;
+}
+
+int enqueue_steps(Handle* h, int n) {
+  for (int s = 0; s < n; ++s) {
+    const float* fin = h->f[h->cur];
+    float* fout = h->f[h->cur ^ 1];
+    CK(launch_nodes(h->dp, fin, h->stream));
+    if (h->fused) {
+      CK(launch_fused(h->dp, fin, fout, h->stream));
+    } else {
+      CK(launch_face_flux(h->dp, fin, h->flux, h->stream));
+      CK(launch_gather(h->dp, fin, h->flux, fout, h->stream));
+    }
+    h->cur ^= 1;
+  }
+  return FVDBM_OK;
+}
+
+int get_graph(Handle* h, int parity, cudaGraphExec_t* out) {
+  if (h->graph[parity]) {
+    *out = h->graph[parity];
+    return FVDBM_OK;
+  }
+  const int save = h->cur;
+  h->cur = parity;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_steps(h, kGraphSteps);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  h->cur = save;
+  if (rc != FVDBM_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(h, FVDBM_ECUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(h, FVDBM_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+  *out = h->graph[parity];
+  return FVDBM_OK;
+}
+
+}  // namespace
+}  // namespace fvdbm
+
+using namespace fvdbm;
+
+extern "C" {
+
+int fvdbm_abi_version(void) { return FVDBM_ABI_VERSION; }
+
+const char* fvdbm_last_error(void* handle) {
+  if (!handle) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    return g_create_err.c_str();
+  }
+  return static_cast<Handle*>(handle)->err.c_str();
+}
+
+int fvdbm_destroy(void* handle) {
+  if (!handle) return FVDBM_OK;
+  Handle* h = static_cast<Handle*>(handle);
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& g : h->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return FVDBM_OK;
+}
+
+int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** handle) {
+  auto create_fail = [&](Handle* h, int code) {
+    {
+      std::lock_guard<std::mutex> lk(g_err_mu);
+      g_create_err = h ? h->err : "invalid arguments";
+    }
+    if (h) fvdbm_destroy(h);
+    return code;
+  };
+  if (!mesh || !params || !handle) return create_fail(nullptr, FVDBM_EINVAL);
+  *handle = nullptr;
+  Handle* h = new Handle();
+  h->params = *params;
+  h->device = params->device;
+  std::string why = build_plan(mesh, params, h->hp);
+  if (!why.empty()) {
+    h->err = why;
+    return create_fail(h, FVDBM_EINVAL);
+  }
+  int rc;
+#define CR(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+      return create_fail(h, FVDBM_ECUDA);                                          \
+    }                                                                              \
+  } while (0)
+  CR(cudaSetDevice(h->device));
+  CR(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  const HostPlan& hp = h->hp;
+  DevPlan& p = h->dp;
+  h->fused = hp.fusable && params->kernel != FVDBM_KERNEL_STAGED;
+  if (params->kernel == FVDBM_KERNEL_FUSED && !hp.fusable) {
+    h->err = "the fused kernel needs every cell face slot to name a face of that cell "
+             "and no per-q flux scale";
+    return create_fail(h, FVDBM_EINVAL);
+  }
+  p.N = hp.N;
+  p.Np = hp.Np;
+  p.F = hp.F;
+  p.Fp = hp.Fp;
+  p.K = hp.K;
+  p.M = hp.M;
+  p.Mp = hp.Mp;
+  p.Mc = hp.Mc;
+  p.scheme = hp.scheme;
+  p.variant = hp.variant;
+  p.fv = hp.fv ? 1 : 0;
+  p.last_cell = hp.last_cell_new;
+  p.inv_tau = params->inv_tau;
+  p.dt = params->delta_t;
+  p.c2 = params->c2;
+  p.c4x2 = params->c4x2;
+  p.c2x2 = params->c2x2;
+
+#define UP(field, vec)                                                        \
+  do {                                                                        \
+    decltype(vec)::value_type* d_ = nullptr;                                  \
+    if ((rc = dalloc(h, &d_, (vec).size(), &(vec))) != FVDBM_OK)              \
+      return create_fail(h, rc);                                              \
+    p.field = d_;                                                             \
+  } while (0)
+  UP(fs0, hp.fs0);
+  UP(fs1, hp.fs1);
+  UP(fnx, hp.fnx);
+  UP(fny, hp.fny);
+  UP(fL, hp.fL);
+  UP(fr, hp.fr);
+  UP(fD2, hp.fD2);
+  UP(fna, hp.fna);
+  UP(fnb, hp.fnb);
+  UP(frl, hp.frl);
+  UP(frr, hp.frr);
+  UP(fkl, hp.fkl);
+  UP(fkr, hp.fkr);
+  UP(fscale, hp.fscale);
+  UP(cf_face, hp.cf_face);
+  UP(cf_sign, hp.cf_sign);
+  if (h->fused) {
+    UP(hf_code, hp.hf_code);
+    UP(hf_nx, hp.hf_nx);
+    UP(hf_ny, hp.hf_ny);
+    UP(hf_L, hp.hf_L);
+    UP(hf_r, hp.hf_r);
+    UP(hf_D2, hp.hf_D2);
+    UP(hf_scale, hp.hf_scale);
+    UP(gh_a, hp.gh_a);
+    UP(gh_b, hp.gh_b);
+    UP(gh_r, hp.gh_r);
+  }
+  UP(nd_type, hp.nd_type);
+  UP(nd_ptr, hp.nd_ptr);
+  UP(nd_npad, hp.nd_npad);
+  UP(nd_cell, hp.nd_cell);
+  UP(nd_w, hp.nd_w);
+  UP(nd_sumw, hp.nd_sumw);
+  UP(inv_area, hp.inv_area);
+  {
+    float* d = nullptr;
+    if ((rc = dalloc<float>(h, &d, size_t(Q) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
+    p.node_pdf = d;
+    if ((rc = dalloc<float>(h, &d, hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
+    p.node_rho = d;
+    if ((rc = dalloc<float>(h, &d, size_t(2) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
+    p.node_vel = d;
+  }
+  for (int b = 0; b < 2; ++b) {
+    if ((rc = dalloc<float>(h, &h->f[b], size_t(Q) * hp.Np)) != FVDBM_OK) return create_fail(h, rc);
+    CR(cudaMemsetAsync(h->f[b], 0, size_t(Q) * hp.Np * 4, h->stream));
+  }
+  if (!h->fused)
+    if ((rc = dalloc<float>(h, &h->flux, size_t(Q) * hp.Fp)) != FVDBM_OK) return create_fail(h, rc);
+  if ((rc = dalloc<float>(h, &h->stage, size_t(Q) * std::max(hp.N, hp.F))) != FVDBM_OK)
+    return create_fail(h, rc);
+  if ((rc = dalloc(h, &h->d_cell_new, hp.cell_new.size(), &hp.cell_new)) != FVDBM_OK)
+    return create_fail(h, rc);
+
+  // rest state: every pdf = feq(1, 0) = W (src/containers.py:29)
+  const float W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 9.0),
+                      (float)(1.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 36.0),
+                      (float)(1.0 / 36.0), (float)(1.0 / 36.0), (float)(1.0 / 36.0)};
+  h->node_pdf.resize(size_t(Q) * hp.P);
+  for (int pp = 0; pp < hp.P; ++pp)
+    for (int q = 0; q < Q; ++q) h->node_pdf[size_t(pp) * Q + q] = W[q];
+  h->node_rho.assign(hp.P, 0.0f);
+  h->node_vel.assign(size_t(2) * hp.P, 0.0f);
+  if ((rc = upload_nodes(h)) != FVDBM_OK) return create_fail(h, rc);
+  {
+    std::vector<float> cells(size_t(Q) * hp.N);
+    for (int c = 0; c < hp.N; ++c)
+      for (int q = 0; q < Q; ++q) cells[size_t(c) * Q + q] = W[q];
+    if ((rc = fvdbm_set_state(h, cells.data(), nullptr, nullptr, nullptr)) != FVDBM_OK)
+      return create_fail(h, rc);
+  }
+  CR(cudaStreamSynchronize(h->stream));
+  *handle = h;
+  return FVDBM_OK;
+#undef CR
+#undef UP
+}
+
+int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, const float* node_rho,
+                    const float* node_vel) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  if (cell_pdf && hp.N > 0) {
+    CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(Q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, hp.Np, h->stream));
+  }
+  if (node_pdf || node_rho || node_vel) {
+    if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(Q) * hp.P * 4);
+    if (node_rho) std::memcpy(h->node_rho.data(), node_rho, size_t(hp.P) * 4);
+    if (node_vel) std::memcpy(h->node_vel.data(), node_vel, size_t(2) * hp.P * 4);
+    int rc = upload_nodes(h);
+    if (rc != FVDBM_OK) return rc;
+  }
+  return FVDBM_OK;
+}
+
+int fvdbm_step(void* handle, int32_t n_steps) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (n_steps < 0) return fail(h, FVDBM_EINVAL, "n_steps < 0");
+  CK(cudaSetDevice(h->device));
+  int n = n_steps;
+  if (n >= kGraphSteps && h->hp.N > 0) {
+    while (n >= kGraphSteps) {
+      cudaGraphExec_t g;
+      int rc = get_graph(h, h->cur, &g);
+      if (rc != FVDBM_OK) return rc;
+      CK(cudaGraphLaunch(g, h->stream));
+      n -= kGraphSteps;  // even: the current buffer is unchanged
+    }
+  }
+  int rc = enqueue_steps(h, n);
+  if (rc != FVDBM_OK) return rc;
+  h->steps_done += n_steps;
+  return FVDBM_OK;
+}
+
+int fvdbm_step_phase(void* handle, int32_t phase) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  CK(cudaSetDevice(h->device));
+  const float* fin = h->f[h->cur];
+  float* fout = h->f[h->cur ^ 1];
+  if (phase == 1) {
+    CK(launch_nodes(h->dp, fin, h->stream));
+  } else if (phase == 2) {
+    if (h->fused) {
+      CK(launch_fused(h->dp, fin, fout, h->stream));
+    } else {
+      CK(launch_face_flux(h->dp, fin, h->flux, h->stream));
+      CK(launch_gather(h->dp, fin, h->flux, fout, h->stream));
+    }
+    h->cur ^= 1;
+    h->steps_done += 1;
+  } else {
+    return fail(h, FVDBM_EINVAL, "phase must be 1 or 2");
+  }
+  return FVDBM_OK;
+}
+
+int fvdbm_sync(void* handle) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  return FVDBM_OK;
+}
+
+int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf_eq) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  const int N = hp.N;
+  const int tb = 256, nb = (N + tb - 1) / tb;
+  if (pdf && N > 0) {
+    k_soa_to_aos<<<nb, tb, 0, h->stream>>>(h->f[h->cur], h->stage, h->d_cell_new, N, hp.Np, Q);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(pdf, h->stage, size_t(Q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  if ((rho || vel || pdf_eq) && N > 0) {
+    if (h->steps_done == 0) {
+      if (rho) std::memset(rho, 0, size_t(N) * 4);
+      if (vel) std::memset(vel, 0, size_t(2) * N * 4);
+      if (pdf_eq) std::memset(pdf_eq, 0, size_t(Q) * N * 4);
+    } else {
+      if (!h->mac) {
+        int rc = dalloc<float>(h, &h->mac, size_t(12) * hp.Np);
+        if (rc != FVDBM_OK) return rc;
+      }
+      float* mr = h->mac;
+      float* mv = h->mac + hp.Np;
+      float* me = h->mac + size_t(3) * hp.Np;
+      CK(launch_macros(h->dp, h->f[h->cur ^ 1], mr, mv, me, h->stream));
+      if (rho) {
+        k_soa_to_aos<<<nb, tb, 0, h->stream>>>(mr, h->stage, h->d_cell_new, N, hp.Np, 1);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(rho, h->stage, size_t(N) * 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+      }
+      if (vel) {
+        k_soa_to_aos<<<nb, tb, 0, h->stream>>>(mv, h->stage, h->d_cell_new, N, hp.Np, 2);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(vel, h->stage, size_t(2) * N * 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+      }
+      if (pdf_eq) {
+        k_soa_to_aos<<<nb, tb, 0, h->stream>>>(me, h->stage, h->d_cell_new, N, hp.Np, Q);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(pdf_eq, h->stage, size_t(Q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+      }
+    }
+  }
+  return FVDBM_OK;
+}
+
+int fvdbm_get_nodes(void* handle, float* pdf, float* rho, float* vel) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  if (hp.M > 0) {
+    std::vector<float> dp(size_t(Q) * hp.Mp), dr(hp.Mp), dv(size_t(2) * hp.Mp);
+    CK(cudaMemcpyAsync(dp.data(), h->dp.node_pdf, dp.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(dr.data(), h->dp.node_rho, dr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(dv.data(), h->dp.node_vel, dv.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int d = 0; d < hp.M; ++d) {
+      const int p = hp.node_orig[d];
+      for (int q = 0; q < Q; ++q) h->node_pdf[size_t(p) * Q + q] = dp[size_t(q) * hp.Mp + d];
+      h->node_rho[p] = dr[d];
+      h->node_vel[size_t(p) * 2] = dv[d];
+      h->node_vel[size_t(p) * 2 + 1] = dv[hp.Mp + d];
+    }
+  }
+  if (pdf) std::memcpy(pdf, h->node_pdf.data(), size_t(Q) * hp.P * 4);
+  if (rho) std::memcpy(rho, h->node_rho.data(), size_t(hp.P) * 4);
+  if (vel) std::memcpy(vel, h->node_vel.data(), size_t(2) * hp.P * 4);
+  return FVDBM_OK;
+}
+
+int fvdbm_get_face_fluxes(void* handle, float* flux) {
+  if (!handle || !flux) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  if (hp.F == 0) return FVDBM_OK;
+  if (!h->flux) {
+    int rc = dalloc<float>(h, &h->flux, size_t(Q) * hp.Fp);
+    if (rc != FVDBM_OK) return rc;
+  }
+  CK(launch_face_flux(h->dp, h->f[h->cur ^ 1], h->flux, h->stream));
+  std::vector<float> soa(size_t(Q) * hp.Fp);
+  CK(cudaMemcpyAsync(soa.data(), h->flux, soa.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int j = 0; j < hp.F; ++j) {
+    const int f = hp.face_old[j];
+    for (int q = 0; q < Q; ++q) flux[size_t(f) * Q + q] = soa[size_t(q) * hp.Fp + j];
+  }
+  return FVDBM_OK;
+}
+
+void* fvdbm_stream(void* handle) { return handle ? static_cast<Handle*>(handle)->stream : nullptr; }
+
+int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
+  if (!handle || !info) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  info->n_cells = hp.N;
+  info->n_faces = hp.F;
+  info->n_nodes = hp.P;
+  info->n_bc_nodes = hp.Mc;
+  info->n_ghost_faces = hp.n_ghost_faces;
+  info->kernel = h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED;
+  info->launches_per_step = (hp.Mc > 0 ? 1 : 0) + (h->fused ? 1 : 2);
+  info->padded_cells = hp.Np;
+  info->bytes_per_step = hp.bytes_per_step;
+  info->device_bytes = h->device_bytes;
+  return FVDBM_OK;
+}
+
+}  // extern "C"

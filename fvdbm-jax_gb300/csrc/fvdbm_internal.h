@@ -1,0 +1,140 @@
+// Internal structures of libfvdbm: the host-side plan built from the
+// reference-layout containers and the device view the kernels read.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace fvdbm {
+
+constexpr int Q = 9;
+
+// Half-face code of the fused kernel (one per cell and face slot):
+//   bits 0-1  sigma + 1   (sigma in {-1,0,1}: Cells.face_normals)
+//   bit  2    this cell is the face's slot 1 (else slot 0)
+//   bit  3    the other slot is a ghost (other = ghost-table index)
+//   bits 4-31 the other cell (device numbering) or the ghost index
+constexpr int HF_SLOT1 = 1 << 2;
+constexpr int HF_GHOST = 1 << 3;
+constexpr int HF_SHIFT = 4;
+constexpr int64_t HF_MAX_INDEX = (int64_t(1) << 27) - 1;
+
+// Node-cell entry: cell index (device numbering); bit 31 marks an entry whose
+// reference index was -1 (its rho/vel gather wraps to the last cell but its
+// non-equilibrium part is zero, src/containers.py:388-390).
+constexpr uint32_t ND_NEQ_ZERO = 0x80000000u;
+
+struct HostPlan {
+  int N = 0, F = 0, P = 0, K = 0, Kn = 0;
+  int Np = 0;  // padded row stride of [9][Np] cell arrays
+  int Fp = 0;  // padded row stride of [9][Fp] face arrays
+  int scheme = 0, variant = 0;
+  bool fv = false;
+  bool fusable = false;
+  int ordering = 0;
+
+  std::vector<int32_t> cell_new;  // old -> new
+  std::vector<int32_t> cell_old;  // new -> old
+  int32_t last_cell_new = 0;      // device id of the reference's cell N-1
+
+  // faces in device order
+  std::vector<int32_t> face_old;  // new -> old
+  std::vector<int32_t> face_new;  // old -> new
+  std::vector<int32_t> fs0, fs1;  // slot cells (device ids) or -1
+  std::vector<float> fnx, fny, fL;
+  std::vector<float> fr, fD2;     // Lax-Wendroff: d0/(d0+d1), 2*(d0+d1)
+  std::vector<int32_t> fna, fnb;  // end nodes (device node ids) for ghosts
+  std::vector<float> frl, frr;    // ghost ratios d0/d1 (slot 0 ghost), d1/d0 (slot 1 ghost)
+  std::vector<int32_t> fkl, fkr;  // known cells of those ghosts
+  std::vector<float> fscale;      // [F] or [9][Fp]
+  int n_ghost_faces = 0;
+
+  // staged gather: [K][Np]
+  std::vector<int32_t> cf_face;
+  std::vector<float> cf_sign;
+
+  // fused half faces: [K][Np]
+  std::vector<int32_t> hf_code;
+  std::vector<float> hf_nx, hf_ny, hf_L, hf_r, hf_D2, hf_scale;
+  std::vector<int32_t> gh_a, gh_b;
+  std::vector<float> gh_r;
+
+  // nodes on the device: computed (type 1/2) first, then frozen ghost ends
+  int M = 0, Mc = 0, Mp = 0;
+  std::vector<int32_t> node_dev;   // reference node -> device id or -1
+  std::vector<int32_t> node_orig;  // device id -> reference node
+  std::vector<int32_t> nd_type, nd_ptr, nd_npad;
+  std::vector<uint32_t> nd_cell;
+  std::vector<float> nd_w, nd_sumw;
+
+  std::vector<float> inv_area;  // [Np] when fv
+
+  double bytes_per_step = 0.0;
+};
+
+struct MeshIn;  // fvdbm_mesh_t
+
+// Build the plan; returns an empty string on success, else the reason.
+std::string build_plan(const void* mesh, const void* params, HostPlan& hp);
+
+struct DevPlan {
+  int N, Np, F, Fp, K, M, Mp, Mc;
+  int scheme, variant, fv;
+  int last_cell;
+  float inv_tau, dt, c2, c4x2, c2x2;
+  // staged faces
+  const int* fs0;
+  const int* fs1;
+  const float* fnx;
+  const float* fny;
+  const float* fL;
+  const float* fr;
+  const float* fD2;
+  const int* fna;
+  const int* fnb;
+  const float* frl;
+  const float* frr;
+  const int* fkl;
+  const int* fkr;
+  const float* fscale;
+  const int* cf_face;
+  const float* cf_sign;
+  // fused half faces
+  const int* hf_code;
+  const float* hf_nx;
+  const float* hf_ny;
+  const float* hf_L;
+  const float* hf_r;
+  const float* hf_D2;
+  const float* hf_scale;
+  const int* gh_a;
+  const int* gh_b;
+  const float* gh_r;
+  // nodes
+  const int* nd_type;
+  const int* nd_ptr;
+  const int* nd_npad;
+  const unsigned* nd_cell;
+  const float* nd_w;
+  const float* nd_sumw;
+  float* node_pdf;  // [9][Mp]
+  float* node_rho;  // [Mp]
+  float* node_vel;  // [2][Mp]
+  const float* inv_area;
+};
+
+// kernel launchers (kernels.cu)
+cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s);
+cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
+cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);
+cudaError_t launch_gather(const DevPlan& p, const float* fin, const float* flux, float* fout,
+                          cudaStream_t s);
+cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
+                          cudaStream_t s);
+cudaError_t launch_scatter_cells(const float* src_aos, float* dst_soa, const int* cell_new, int N,
+                                 int Np, cudaStream_t s);
+
+}  // namespace fvdbm

@@ -1,0 +1,413 @@
+// Host-side plan: validates the reference-layout containers, renumbers the
+// cells for locality and builds every device table.  Float32 quantities that
+// the reference evaluates inside the step but that depend only on static
+// data (IDW weights 1/d, their sum, the Lax-Wendroff d0/(d0+d1), the ghost
+// distance ratios) are evaluated here once with the same float32 operations,
+// so the kernels stay bitwise equal to the per-step evaluation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <sstream>
+
+#include "../../include/fvdbm.h"
+#include "fvdbm_internal.h"
+
+namespace fvdbm {
+
+namespace {
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// JAX gathers wrap index -1 to the last row (the reference pads with -1).
+inline int32_t wrap(int32_t idx, int32_t n) { return idx < 0 ? idx + n : idx; }
+
+uint32_t spread16(uint32_t x) {
+  x &= 0xffff;
+  x = (x | (x << 8)) & 0x00ff00ff;
+  x = (x | (x << 4)) & 0x0f0f0f0f;
+  x = (x | (x << 2)) & 0x33333333;
+  x = (x | (x << 1)) & 0x55555555;
+  return x;
+}
+
+std::vector<int32_t> morton_order(const float* xy, int N) {
+  float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+  for (int i = 0; i < N; ++i) {
+    x0 = std::min(x0, xy[2 * i]);
+    x1 = std::max(x1, xy[2 * i]);
+    y0 = std::min(y0, xy[2 * i + 1]);
+    y1 = std::max(y1, xy[2 * i + 1]);
+  }
+  const double span = std::max(double(x1 - x0), double(y1 - y0));
+  const double s = span > 0 ? 65535.0 / span : 0.0;
+  std::vector<std::pair<uint32_t, int32_t>> key(N);
+  for (int i = 0; i < N; ++i) {
+    uint32_t qx = uint32_t(std::min(65535.0, std::max(0.0, (xy[2 * i] - x0) * s)));
+    uint32_t qy = uint32_t(std::min(65535.0, std::max(0.0, (xy[2 * i + 1] - y0) * s)));
+    key[i] = {spread16(qx) | (spread16(qy) << 1), i};
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int32_t> order(N);
+  for (int i = 0; i < N; ++i) order[i] = key[i].second;
+  return order;
+}
+
+// Reverse Cuthill-McKee over the cell adjacency given by interior faces.
+std::vector<int32_t> rcm_order(int N, int F, const int32_t* fc) {
+  std::vector<int32_t> deg(N, 0);
+  for (int f = 0; f < F; ++f) {
+    const int a = fc[2 * f], b = fc[2 * f + 1];
+    if (a >= 0 && b >= 0 && a != b) {
+      deg[a]++;
+      deg[b]++;
+    }
+  }
+  std::vector<int32_t> ptr(N + 1, 0);
+  for (int i = 0; i < N; ++i) ptr[i + 1] = ptr[i] + deg[i];
+  std::vector<int32_t> adj(ptr[N]);
+  std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (int f = 0; f < F; ++f) {
+    const int a = fc[2 * f], b = fc[2 * f + 1];
+    if (a >= 0 && b >= 0 && a != b) {
+      adj[fill[a]++] = b;
+      adj[fill[b]++] = a;
+    }
+  }
+  for (int i = 0; i < N; ++i)
+    std::sort(adj.begin() + ptr[i], adj.begin() + ptr[i + 1],
+              [&](int x, int y) { return deg[x] != deg[y] ? deg[x] < deg[y] : x < y; });
+  std::vector<int32_t> order;
+  order.reserve(N);
+  std::vector<char> seen(N, 0);
+  std::vector<int32_t> by_deg(N);
+  std::iota(by_deg.begin(), by_deg.end(), 0);
+  std::stable_sort(by_deg.begin(), by_deg.end(), [&](int x, int y) { return deg[x] < deg[y]; });
+  for (int start : by_deg) {
+    if (seen[start]) continue;
+    // pseudo-peripheral start: last node of a BFS from the min-degree node
+    int s = start;
+    {
+      std::vector<int32_t> lvl;
+      std::queue<int32_t> qq;
+      std::vector<char> vis(0);
+      qq.push(s);
+      std::vector<int32_t> visited{ s };
+      seen[s] = 2;
+      int last = s;
+      while (!qq.empty()) {
+        int u = qq.front();
+        qq.pop();
+        last = u;
+        for (int e = ptr[u]; e < ptr[u + 1]; ++e)
+          if (!seen[adj[e]]) {
+            seen[adj[e]] = 2;
+            visited.push_back(adj[e]);
+            qq.push(adj[e]);
+          }
+      }
+      for (int v : visited) seen[v] = 0;
+      s = last;
+    }
+    std::queue<int32_t> qq;
+    qq.push(s);
+    seen[s] = 1;
+    while (!qq.empty()) {
+      int u = qq.front();
+      qq.pop();
+      order.push_back(u);
+      for (int e = ptr[u]; e < ptr[u + 1]; ++e)
+        if (!seen[adj[e]]) {
+          seen[adj[e]] = 1;
+          qq.push(adj[e]);
+        }
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  return order;
+}
+
+}  // namespace
+
+std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
+  const fvdbm_mesh_t& m = *static_cast<const fvdbm_mesh_t*>(mesh_v);
+  const fvdbm_params_t& pr = *static_cast<const fvdbm_params_t*>(params_v);
+  std::ostringstream err;
+  const int N = m.n_cells, F = m.n_faces, P = m.n_nodes, K = m.cell_face_stride,
+            Kn = m.node_cell_stride;
+  if (N < 0 || F < 0 || P < 0 || K < 0 || Kn < 0) return "negative size";
+  if (int64_t(N) > HF_MAX_INDEX || int64_t(F) > HF_MAX_INDEX) return "mesh too large (max 2^27 cells/faces)";
+  if (pr.flux_scheme != FVDBM_UPWIND && pr.flux_scheme != FVDBM_LAX_WENDROFF)
+    return "Unknown flux scheme";
+  if (pr.variant < 0 || pr.variant > 2) return "unknown flux variant";
+  if (N > 0 && K > 0 && (!m.cell_face_indices || !m.cell_face_signs)) return "cell face arrays missing";
+  if (F > 0 && (!m.face_cells || !m.face_dists || !m.face_nodes || !m.face_n || !m.face_L))
+    return "face arrays missing";
+  if (P > 0 && (!m.node_type || (Kn > 0 && (!m.node_cells || !m.node_dists))))
+    return "node arrays missing";
+  if (pr.variant != 0 && F > 0 && !m.face_scale) return "face_scale missing for the flux variant";
+  if (K > 0 && N > 0 && F == 0) return "cells reference faces but there are none";
+
+  hp.N = N;
+  hp.F = F;
+  hp.P = P;
+  hp.K = K;
+  hp.Kn = Kn;
+  hp.Np = std::max(128, round_up(N, 128));
+  hp.Fp = std::max(128, round_up(F, 128));
+  hp.scheme = pr.flux_scheme;
+  hp.variant = pr.variant;
+  hp.fv = m.cell_inv_area != nullptr;
+
+  // ---- validation (reference semantics: -1 wraps to the last row)
+  for (int64_t t = 0; t < int64_t(N) * K; ++t) {
+    const int32_t fi = m.cell_face_indices[t], sg = m.cell_face_signs[t];
+    if (fi < -1 || fi >= F) {
+      err << "Cells.face_indices[" << t / K << "," << t % K << "]=" << fi << " out of range";
+      return err.str();
+    }
+    if (sg < -1 || sg > 1) {
+      err << "Cells.face_normals[" << t / K << "," << t % K << "]=" << sg << " is not -1, 0 or 1";
+      return err.str();
+    }
+  }
+  for (int64_t t = 0; t < int64_t(F) * 2; ++t) {
+    if (m.face_cells[t] < -1 || m.face_cells[t] >= N) {
+      err << "Faces.stencil_cells_index[" << t / 2 << "," << t % 2 << "] out of range";
+      return err.str();
+    }
+    if (m.face_nodes[t] < -1 || m.face_nodes[t] >= P) {
+      err << "Faces.nodes_index[" << t / 2 << "," << t % 2 << "] out of range";
+      return err.str();
+    }
+  }
+  for (int p = 0; p < P; ++p) {
+    const int t = m.node_type[p];
+    if (t < 0 || t > 2) {
+      err << "Nodes.type[" << p << "]=" << t << " is not 0, 1 or 2";
+      return err.str();
+    }
+    for (int k = 0; k < Kn; ++k)
+      if (m.node_cells[int64_t(p) * Kn + k] < -1 || m.node_cells[int64_t(p) * Kn + k] >= N) {
+        err << "Nodes.cells_index[" << p << "," << k << "] out of range";
+        return err.str();
+      }
+  }
+
+  // ---- cell order
+  hp.ordering = pr.ordering;
+  if (pr.ordering == FVDBM_ORDER_MORTON && m.cell_xy && N > 0)
+    hp.cell_old = morton_order(m.cell_xy, N);
+  else if (pr.ordering == FVDBM_ORDER_RCM && N > 0)
+    hp.cell_old = rcm_order(N, F, m.face_cells);
+  else {
+    hp.cell_old.resize(N);
+    std::iota(hp.cell_old.begin(), hp.cell_old.end(), 0);
+    if (pr.ordering == FVDBM_ORDER_MORTON) hp.ordering = FVDBM_ORDER_NONE;
+  }
+  hp.cell_new.assign(N, -1);
+  for (int i = 0; i < N; ++i) hp.cell_new[hp.cell_old[i]] = i;
+  hp.last_cell_new = N > 0 ? hp.cell_new[N - 1] : 0;
+  auto cnew = [&](int32_t c) { return c < 0 ? -1 : hp.cell_new[c]; };
+  auto cnew_wrap = [&](int32_t c) { return N > 0 ? hp.cell_new[wrap(c, N)] : 0; };
+
+  // ---- which faces need ghosts, which nodes live on the device
+  std::vector<char> ghost_face(F, 0);
+  for (int f = 0; f < F; ++f)
+    ghost_face[f] = (m.face_cells[2 * f] == -1 || m.face_cells[2 * f + 1] == -1);
+  hp.n_ghost_faces = int(std::count(ghost_face.begin(), ghost_face.end(), 1));
+  std::vector<char> needed(P, 0);
+  for (int f = 0; f < F; ++f)
+    if (ghost_face[f] && P > 0) {
+      needed[wrap(m.face_nodes[2 * f], P)] = 1;
+      needed[wrap(m.face_nodes[2 * f + 1], P)] = 1;
+    }
+  if (hp.n_ghost_faces > 0 && P == 0) return "faces need ghost nodes but there are no nodes";
+
+  // computed nodes first, ordered by their lowest neighbour cell
+  std::vector<std::pair<int64_t, int32_t>> comp;
+  std::vector<int32_t> frozen;
+  for (int p = 0; p < P; ++p) {
+    if (m.node_type[p] != 0) {
+      int64_t key = int64_t(1) << 40;
+      for (int k = 0; k < Kn; ++k) {
+        const int32_t c = m.node_cells[int64_t(p) * Kn + k];
+        if (c >= 0) key = std::min<int64_t>(key, hp.cell_new[c]);
+      }
+      comp.push_back({key * (int64_t(P) + 1) + p, p});
+    } else if (needed[p]) {
+      frozen.push_back(p);
+    }
+  }
+  std::sort(comp.begin(), comp.end());
+  hp.Mc = int(comp.size());
+  hp.M = hp.Mc + int(frozen.size());
+  hp.Mp = std::max(32, round_up(hp.M, 32));
+  hp.node_dev.assign(P, -1);
+  hp.node_orig.clear();
+  for (auto& c : comp) hp.node_orig.push_back(c.second);
+  for (int p : frozen) hp.node_orig.push_back(p);
+  for (int d = 0; d < hp.M; ++d) hp.node_dev[hp.node_orig[d]] = d;
+
+  // node IDW tables: w = 1/d with negative weights zeroed, sum(w) folded
+  // over all Kn entries in order (utils/utils.py:34-60)
+  hp.nd_type.resize(hp.Mc);
+  hp.nd_ptr.assign(hp.Mc + 1, 0);
+  hp.nd_npad.assign(hp.Mc, 0);
+  hp.nd_sumw.resize(hp.Mc);
+  hp.nd_cell.clear();
+  hp.nd_w.clear();
+  for (int d = 0; d < hp.Mc; ++d) {
+    const int p = hp.node_orig[d];
+    hp.nd_type[d] = m.node_type[p];
+    float sumw = 0.0f;
+    for (int k = 0; k < Kn; ++k) {
+      const int32_t c = m.node_cells[int64_t(p) * Kn + k];
+      const float dist = m.node_dists[int64_t(p) * Kn + k];
+      float w = 1.0f / dist;
+      if (w < 0.0f) w = 0.0f;
+      sumw = (k == 0) ? w : sumw + w;
+      if (c == -1 && w == 0.0f) {
+        hp.nd_npad[d]++;
+        continue;
+      }
+      if (N == 0) return "nodes reference cells but there are none";
+      uint32_t code = uint32_t(cnew_wrap(c));
+      if (c == -1) code |= ND_NEQ_ZERO;
+      hp.nd_cell.push_back(code);
+      hp.nd_w.push_back(w);
+    }
+    hp.nd_sumw[d] = sumw;
+    hp.nd_ptr[d + 1] = int(hp.nd_cell.size());
+  }
+
+  // ---- faces in device order (by lowest slot cell)
+  {
+    std::vector<std::pair<int64_t, int32_t>> fk(F);
+    for (int f = 0; f < F; ++f) {
+      int64_t a = cnew(m.face_cells[2 * f]), b = cnew(m.face_cells[2 * f + 1]);
+      int64_t lo = (a < 0) ? b : (b < 0 ? a : std::min(a, b));
+      if (lo < 0) lo = int64_t(1) << 40;
+      fk[f] = {lo * (int64_t(F) + 1) + f, f};
+    }
+    std::sort(fk.begin(), fk.end());
+    hp.face_old.resize(F);
+    hp.face_new.resize(F);
+    for (int j = 0; j < F; ++j) {
+      hp.face_old[j] = fk[j].second;
+      hp.face_new[fk[j].second] = j;
+    }
+  }
+  hp.fs0.resize(F);
+  hp.fs1.resize(F);
+  hp.fnx.resize(F);
+  hp.fny.resize(F);
+  hp.fL.resize(F);
+  hp.fr.assign(F, 0.0f);
+  hp.fD2.assign(F, 1.0f);
+  hp.fna.assign(F, 0);
+  hp.fnb.assign(F, 0);
+  hp.frl.assign(F, 0.0f);
+  hp.frr.assign(F, 0.0f);
+  hp.fkl.assign(F, 0);
+  hp.fkr.assign(F, 0);
+  if (pr.variant == 1) hp.fscale.assign(F, 1.0f);
+  if (pr.variant == 2) hp.fscale.assign(size_t(Q) * hp.Fp, 1.0f);
+  for (int j = 0; j < F; ++j) {
+    const int f = hp.face_old[j];
+    const int32_t s0 = m.face_cells[2 * f], s1 = m.face_cells[2 * f + 1];
+    const float d0 = m.face_dists[2 * f], d1 = m.face_dists[2 * f + 1];
+    hp.fs0[j] = cnew(s0);
+    hp.fs1[j] = cnew(s1);
+    hp.fnx[j] = m.face_n[2 * f];
+    hp.fny[j] = m.face_n[2 * f + 1];
+    hp.fL[j] = m.face_L[f];
+    const float D = d0 + d1;
+    hp.fr[j] = d0 / D;
+    hp.fD2[j] = 2.0f * D;
+    if (ghost_face[f]) {
+      hp.fna[j] = hp.node_dev[wrap(m.face_nodes[2 * f], P)];
+      hp.fnb[j] = hp.node_dev[wrap(m.face_nodes[2 * f + 1], P)];
+      hp.frl[j] = d0 / d1;
+      hp.frr[j] = d1 / d0;
+      hp.fkl[j] = cnew_wrap(s1);
+      hp.fkr[j] = cnew_wrap(s0);
+    }
+    if (pr.variant == 1) hp.fscale[j] = m.face_scale[f];
+    if (pr.variant == 2)
+      for (int q = 0; q < Q; ++q) hp.fscale[size_t(q) * hp.Fp + j] = m.face_scale[size_t(f) * Q + q];
+  }
+
+  // ---- per-cell face slots: staged gather and fused half faces
+  hp.cf_face.assign(size_t(K) * hp.Np, 0);
+  hp.cf_sign.assign(size_t(K) * hp.Np, 0.0f);
+  hp.fusable = (pr.variant != 2);
+  for (int c = 0; c < N && hp.fusable; ++c)
+    for (int k = 0; k < K; ++k) {
+      const int f = wrap(m.cell_face_indices[int64_t(c) * K + k], F);
+      const int32_t s0 = m.face_cells[2 * f], s1 = m.face_cells[2 * f + 1];
+      if (!((s0 == c) ^ (s1 == c))) {
+        hp.fusable = false;
+        break;
+      }
+    }
+  if (hp.fusable) {
+    hp.hf_code.assign(size_t(K) * hp.Np, 0);
+    hp.hf_nx.assign(size_t(K) * hp.Np, 0.0f);
+    hp.hf_ny.assign(size_t(K) * hp.Np, 0.0f);
+    hp.hf_L.assign(size_t(K) * hp.Np, 0.0f);
+    if (pr.flux_scheme == FVDBM_LAX_WENDROFF) {
+      hp.hf_r.assign(size_t(K) * hp.Np, 0.0f);
+      hp.hf_D2.assign(size_t(K) * hp.Np, 1.0f);
+    }
+    if (pr.variant == 1) hp.hf_scale.assign(size_t(K) * hp.Np, 1.0f);
+  }
+  for (int i = 0; i < N; ++i) {
+    const int c = hp.cell_old[i];
+    for (int k = 0; k < K; ++k) {
+      const int f = wrap(m.cell_face_indices[int64_t(c) * K + k], F);
+      const int32_t sg = m.cell_face_signs[int64_t(c) * K + k];
+      const size_t s = size_t(k) * hp.Np + i;
+      const int j = hp.face_new[f];
+      hp.cf_face[s] = j;
+      hp.cf_sign[s] = float(sg);
+      if (!hp.fusable) continue;
+      const int32_t s0 = m.face_cells[2 * f], s1 = m.face_cells[2 * f + 1];
+      const bool slot1 = (s1 == c);
+      const int32_t oth = slot1 ? s0 : s1;
+      int32_t code = (sg + 1) | (slot1 ? HF_SLOT1 : 0);
+      if (oth == -1) {
+        const int g = int(hp.gh_a.size());
+        hp.gh_a.push_back(hp.fna[j]);
+        hp.gh_b.push_back(hp.fnb[j]);
+        hp.gh_r.push_back(slot1 ? hp.frl[j] : hp.frr[j]);
+        code |= HF_GHOST | (g << HF_SHIFT);
+      } else {
+        code |= hp.cell_new[oth] << HF_SHIFT;
+      }
+      hp.hf_code[s] = code;
+      hp.hf_nx[s] = hp.fnx[j];
+      hp.hf_ny[s] = hp.fny[j];
+      hp.hf_L[s] = hp.fL[j];
+      if (pr.flux_scheme == FVDBM_LAX_WENDROFF) {
+        hp.hf_r[s] = hp.fr[j];
+        hp.hf_D2[s] = hp.fD2[j];
+      }
+      if (pr.variant == 1) hp.hf_scale[s] = hp.fscale[j];
+    }
+  }
+  if (hp.fv) {
+    hp.inv_area.assign(hp.Np, 0.0f);
+    for (int i = 0; i < N; ++i) hp.inv_area[i] = m.cell_inv_area[hp.cell_old[i]];
+  }
+
+  // algorithmic bytes of one step: pdf read+write, cell->face slots, face
+  // geometry (2 slot ints + n + L, + 2 distances for Lax-Wendroff) and the
+  // boundary-node pdf write + read
+  hp.bytes_per_step = 72.0 * N + 4.0 * K * N + 20.0 * F +
+                      (pr.flux_scheme == FVDBM_LAX_WENDROFF ? 8.0 * F : 0.0) + 72.0 * hp.Mc;
+  return "";
+}
+
+}  // namespace fvdbm

@@ -240,6 +240,10 @@ class Mesher:
         cells = Cells(N, dynamics)
         cells.face_indices = self.cell_face_indices.astype(I32)
         cells.face_normals = self.cell_face_normal_signs.astype(I32)
+        # not part of the reference containers: centroids (for the locality
+        # order of the device numbering) and areas (finite-volume mode, mass)
+        cells.centroids = self.cell_centers.astype(F32)
+        cells.areas = self.cell_areas.astype(F32)
 
         scheme = "lax_wendroff" if flux_method in ("lax_wendroff", "cc_lax_wendroff") else "upwind"
         faces = Faces(F, dynamics, flux_scheme=scheme)

@@ -1,0 +1,170 @@
+/*
+ * fvdbm.h - C ABI of the GB300 FVDBM time stepper (libfvdbm.so).
+ *
+ * This is the drop-in boundary for the reference's Environment.init/step
+ * (MADALERAU/FVDBM-JAX src/environment.py:38-42 and :55-65) acting on the
+ * Cells/Faces/Nodes containers that Mesher.to_env builds
+ * (src/mesher.py:610-693) and set_vel_node/set_rho_node mutate
+ * (src/mesher.py:697-742).  The reference binds this path from Python, so the
+ * binding is ctypes (fvdbm-jax_gb300/_native.py); every argument is a plain
+ * pointer or size.
+ *
+ * Conventions
+ *   - Return codes: 0 ok, negative on error (FVDBM_E*); the message is in
+ *     fvdbm_last_error(handle) (or fvdbm_last_error(NULL) for create).
+ *   - Host arrays are read during the call and never retained.  The handle
+ *     owns its device memory and its CUDA stream.  One handle is driven from
+ *     one host thread at a time.
+ *   - Arrays are in the reference's element order and row-major layout; the
+ *     library renumbers cells internally and undoes it on every read-back.
+ *   - fvdbm_step is stream-ordered and returns before the GPU finishes; the
+ *     read-back calls synchronise.
+ *   - No atomics on the step path: results are bitwise run-to-run stable and
+ *     match the CPU oracle bit for bit.
+ */
+#ifndef FVDBM_H
+#define FVDBM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FVDBM_ABI_VERSION 1
+
+#define FVDBM_OK 0
+#define FVDBM_EINVAL (-1)  /* invalid argument or inconsistent mesh */
+#define FVDBM_ECUDA (-2)   /* CUDA runtime error */
+#define FVDBM_ENOMEM (-3)  /* allocation failed */
+#define FVDBM_EDEVICE (-4) /* device-side status word set */
+
+/* Faces.flux_scheme (src/containers.py:197-203) */
+#define FVDBM_UPWIND 0
+#define FVDBM_LAX_WENDROFF 1
+
+/* Flux multipliers of the cell-centre stencil face classes:
+ * FACE_SCALE   = CCStencilFaces, flux * cos(alpha)      (src/faces.py:54-74)
+ * FACE_Q_SCALE = CCStencilKsiFaces, flux * (xi.n)/(xi.npq), q0 -> 0
+ *                                                       (src/faces.py:119-141) */
+#define FVDBM_VARIANT_NONE 0
+#define FVDBM_VARIANT_FACE_SCALE 1
+#define FVDBM_VARIANT_FACE_Q_SCALE 2
+
+/* Cell numbering used on the device (results are always returned in the
+ * caller's order). */
+#define FVDBM_ORDER_NONE 0
+#define FVDBM_ORDER_RCM 1    /* reverse Cuthill-McKee on the face graph */
+#define FVDBM_ORDER_MORTON 2 /* Z-order of cell_xy (needs cell_xy) */
+
+/* Kernel family for the step. */
+#define FVDBM_KERNEL_AUTO 0   /* fused when the mesh allows it, else staged */
+#define FVDBM_KERNEL_STAGED 1 /* node BC + face flux + cell gather (3 kernels) */
+#define FVDBM_KERNEL_FUSED 2  /* node BC + fused cell kernel (2 kernels) */
+
+/* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
+typedef struct fvdbm_mesh {
+  int32_t n_cells;
+  int32_t n_faces;
+  int32_t n_nodes;
+  int32_t cell_face_stride;          /* K: columns of Cells.face_indices */
+  int32_t node_cell_stride;          /* Kn: columns of Nodes.cells_index */
+  const int32_t *cell_face_indices;  /* [N][K] Cells.face_indices, -1 padded */
+  const int32_t *cell_face_signs;    /* [N][K] Cells.face_normals (-1,0,1) */
+  const int32_t *face_cells;         /* [F][2] Faces.stencil_cells_index, -1 = ghost */
+  const float *face_dists;           /* [F][2] Faces.stencil_dists */
+  const int32_t *face_nodes;         /* [F][2] Faces.nodes_index */
+  const float *face_n;               /* [F][2] Faces.n */
+  const float *face_L;               /* [F]    Faces.L */
+  const float *face_scale;           /* [F] (FACE_SCALE) or [F][9] (FACE_Q_SCALE), else NULL */
+  const int32_t *node_type;          /* [P] Nodes.type: 0 none, 1 velocity, 2 density */
+  const int32_t *node_cells;         /* [P][Kn] Nodes.cells_index, -1 padded */
+  const float *node_dists;           /* [P][Kn] Nodes.cell_dists, -1 padded */
+  const float *cell_xy;              /* [N][2] cell centroids for MORTON, or NULL */
+  const float *cell_inv_area;        /* [N] 1/area to scale the flux sum, or NULL
+                                        (NULL = the reference's update, no area) */
+} fvdbm_mesh_t;
+
+/* Step parameters, all float32 as the reference evaluates them
+ * (src/dynamics.py:64-74, src/containers.py:121). */
+typedef struct fvdbm_params {
+  int32_t flux_scheme; /* FVDBM_UPWIND | FVDBM_LAX_WENDROFF */
+  int32_t variant;     /* FVDBM_VARIANT_* */
+  float inv_tau;       /* float32(1/tau), 1/tau taken in double */
+  float delta_t;       /* float32(delta_t) */
+  float c2;            /* C*C with C = 1/sqrt(3) in float32 */
+  float c4x2;          /* 2*((C*C)*(C*C)) */
+  float c2x2;          /* 2*(C*C) */
+  int32_t ordering;    /* FVDBM_ORDER_* */
+  int32_t kernel;      /* FVDBM_KERNEL_* */
+  int32_t device;      /* CUDA device ordinal */
+} fvdbm_params_t;
+
+/* Sizes and the algorithmic traffic of one step, for reporting. */
+typedef struct fvdbm_info {
+  int32_t n_cells, n_faces, n_nodes;
+  int32_t n_bc_nodes;       /* type 1/2 nodes updated each step */
+  int32_t n_ghost_faces;    /* faces with a ghost slot */
+  int32_t kernel;           /* family actually used */
+  int32_t launches_per_step;
+  int32_t padded_cells;     /* row stride of the [9][Np] pdf */
+  double bytes_per_step;    /* algorithmic bytes of one step */
+  double device_bytes;      /* device memory held by the handle */
+} fvdbm_info_t;
+
+/* Environment.init (src/environment.py:38-42): validate the containers,
+ * renumber, build the device tables and upload the rest state
+ * (every pdf = feq(1,0) = W, src/containers.py:29).  Replaces the jit
+ * trace of the first Environment.step. */
+int fvdbm_create(const fvdbm_mesh_t *mesh, const fvdbm_params_t *params, void **handle);
+
+/* The dynamic pytree leaves (Cells.pdf, Nodes.pdf/rho/vel,
+ * src/containers.py:33-36,75,321).  NULL leaves are left unchanged.
+ * cell_pdf [N][9], node_pdf [P][9], node_rho [P], node_vel [P][2]. */
+int fvdbm_set_state(void *handle, const float *cell_pdf, const float *node_pdf,
+                    const float *node_rho, const float *node_vel);
+
+/* n_steps applications of Environment.step (src/environment.py:55-65). */
+int fvdbm_step(void *handle, int32_t n_steps);
+
+/* One step split at its kernel boundary so a caller can time each kernel
+ * with events on fvdbm_stream(): phase 1 launches the boundary-node kernel
+ * (Nodes.calc_pdfs), phase 2 the cell kernel(s) (Faces.calc_fluxes +
+ * Cells.calc_pdfs) and completes the step.  Phase 1 then phase 2 is exactly
+ * fvdbm_step(handle, 1). */
+int fvdbm_step_phase(void *handle, int32_t phase);
+
+/* Cells.pdf after the last step, and Cells.rho/vel/pdf_eq as the reference
+ * leaves them: the macros of the pdf before the last update
+ * (src/environment.py:60-64).  Any pointer may be NULL.  Synchronises.
+ * pdf [N][9], rho [N], vel [N][2], pdf_eq [N][9]. */
+int fvdbm_get_cells(void *handle, float *pdf, float *rho, float *vel, float *pdf_eq);
+
+/* Nodes.pdf/rho/vel after the last step.  pdf [P][9], rho [P], vel [P][2]. */
+int fvdbm_get_nodes(void *handle, float *pdf, float *rho, float *vel);
+
+/* Faces.pdf after the last step: the face fluxes of the last update
+ * (src/containers.py:205-213).  flux [F][9]. */
+int fvdbm_get_face_fluxes(void *handle, float *flux);
+
+/* Block until the handle's stream is idle; returns the device status. */
+int fvdbm_sync(void *handle);
+
+/* The handle's cudaStream_t (for event timing by the caller). */
+void *fvdbm_stream(void *handle);
+
+int fvdbm_get_info(void *handle, fvdbm_info_t *info);
+
+/* Message of the last failure on this handle (or of the last failed create
+ * when handle is NULL). */
+const char *fvdbm_last_error(void *handle);
+
+int fvdbm_destroy(void *handle);
+
+int fvdbm_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FVDBM_H */

@@ -67,3 +67,44 @@ def inv_tau_dt(g):
     tau = float(g["tau"])
     dt = float(g["delta_t"])
     return np.float32(1 / tau), np.float32(dt)
+
+
+def containers(g):
+    """Host containers (this package's) holding a golden case's reference
+    containers and initial state."""
+    from fvdbm_jax_gb300.containers import Cells, Faces, Nodes
+    from fvdbm_jax_gb300.dynamics import D2Q9
+
+    scheme, variant = SCHEMES[str(g["flux_method"])]
+    dyn = D2Q9(float(g["tau"]), float(g["delta_t"]))
+    N, F, P = g["s0_c_pdf"].shape[0], g["s0_f_pdf"].shape[0], g["s0_n_pdf"].shape[0]
+    c = Cells(N, dyn)
+    c.face_indices = g["c_face_indices"].astype(np.int32)
+    c.face_normals = g["c_face_normals"].astype(np.int32)
+    c.pdf, c.rho, c.vel, c.pdf_eq = g["s0_c_pdf"], g["s0_c_rho"], g["s0_c_vel"], g["s0_c_pdf_eq"]
+    f = Faces(F, dyn, scheme)
+    f.pdf = g["s0_f_pdf"]
+    f.stencil_cells_index = g["f_stencil_cells_index"].astype(np.int32)
+    f.stencil_dists = g["f_stencil_dists"].astype(np.float32)
+    f.nodes_index = g["f_nodes_index"].astype(np.int32)
+    f.n = g["f_n"].astype(np.float32)
+    f.L = g["f_L"].astype(np.float32).reshape(-1, 1)
+    f.stencil_variant = variant
+    if variant == "cos":
+        f.alpha = g["f_alpha"].astype(np.float32).reshape(-1, 1)
+    if variant == "ksi":
+        f.npq = g["f_npq"].astype(np.float32).reshape(-1, 2)
+    n = Nodes(P, dyn)
+    n.pdf, n.rho, n.vel = g["s0_n_pdf"], g["s0_n_rho"], g["s0_n_vel"]
+    n.type = g["n_type"].astype(np.int32).reshape(-1, 1)
+    n.cells_index = g["n_cells_index"].astype(np.int32)
+    n.cell_dists = g["n_cell_dists"].astype(np.float32)
+    return c, f, n
+
+
+def env_state(env):
+    """The reference-visible state of an Environment as a flat dict."""
+    return {"cells_pdf": np.array(env.cells.pdf), "cells_rho": np.array(env.cells.rho),
+            "cells_vel": np.array(env.cells.vel), "cells_pdf_eq": np.array(env.cells.pdf_eq),
+            "faces_pdf": np.array(env.faces.pdf), "nodes_pdf": np.array(env.nodes.pdf),
+            "nodes_rho": np.array(env.nodes.rho), "nodes_vel": np.array(env.nodes.vel)}
