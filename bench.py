@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="porous1m", choices=["porous1m", "cavity", "channel"])
+    ap.add_argument("--workload", default="porous1m",
+                    choices=["porous1m", "porous2m", "porous4m", "cavity", "channel"])
     ap.add_argument("--flux", default="upwind", choices=["upwind", "lax_wendroff"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -55,8 +56,9 @@ def parse():
 def workload(name, flux, seed):
     from fvdbm_jax_gb300 import D2Q9, Mesher, meshgen
     t0 = time.perf_counter()
-    if name == "porous1m":
-        raw = meshgen.porous(n_obstacles=400, n_target=1_000_000, porosity=0.70, seed=seed)
+    if name.startswith("porous"):
+        target = {"porous1m": 1_000_000, "porous2m": 2_000_000, "porous4m": 4_000_000}[name]
+        raw = meshgen.porous(n_obstacles=400, n_target=target, porosity=0.70, seed=seed)
         tau = 0.6
     elif name == "channel":
         raw = meshgen.channel_cylinder(seed=seed)
@@ -68,7 +70,7 @@ def workload(name, flux, seed):
     m.calc_mesh_properties()
     dyn = D2Q9(tau, 0.5 * float(m.face_lengths.min()))
     c, f, n = m.to_env(dyn, flux)
-    if name == "porous1m":
+    if name.startswith("porous"):
         for mk in (1, 3, 5):
             n = m.set_vel_node(n, mk, (0.0, 0.0))
         n = m.set_rho_node(n, 4, 1.001)
@@ -89,11 +91,13 @@ def workload(name, flux, seed):
             n = m.set_vel_node(n, mk, (0.0, 0.0))
         n = m.set_vel_node(n, 3, (0.1, 0.0))
     desc = {"workload": {"porous1m": "porous square, 400 obstacles, ~1M triangles",
+                         "porous2m": "porous square, 400 obstacles, ~2M triangles",
+                         "porous4m": "porous square, 400 obstacles, ~4M triangles",
                          "channel": "channel 2.2x0.41 with cylinder, ~60k triangles",
                          "cavity": "lid-driven cavity 41x41 grid, 3,200 triangles"}[name],
             "cells": int(c.pdf.shape[0]), "faces": int(f.pdf.shape[0]), "nodes": int(n.pdf.shape[0]),
             "lattice": "D2Q9", "flux": flux, "tau": tau, "delta_t": float(dyn.delta_t),
-            "porosity": float(raw.info.get("porosity", 1.0)) if name == "porous1m" else None,
+            "porosity": float(raw.info.get("porosity", 1.0)) if name.startswith("porous") else None,
             "seed": seed, "setup_s": round(time.perf_counter() - t0, 2)}
     return m, dyn, c, f, n, desc
 

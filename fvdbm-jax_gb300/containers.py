@@ -114,7 +114,8 @@ def _arr(x, dtype):
 
 
 def from_any(cells, faces, nodes, dynamics=None):
-    """Copy reference (or these) containers into fresh host containers.
+    """Copy reference (or these) containers into fresh host containers; the
+    originals are never modified.
     Flux-scheme variants are recognised by the reference's class names
     ``CCStencilFaces`` (``alpha``) and ``CCStencilKsiFaces`` (``npq``)."""
     dyn = dynamics or getattr(cells, "dynamics", None)
@@ -132,6 +133,9 @@ def from_any(cells, faces, nodes, dynamics=None):
     c.pdf_eq = _arr(cells.pdf_eq, F32).reshape(N, 9)
     c.face_indices = _arr(cells.face_indices, I32).reshape(N, -1)
     c.face_normals = _arr(cells.face_normals, I32).reshape(N, -1)
+    for extra in ("centroids", "areas"):
+        if getattr(cells, extra, None) is not None:
+            setattr(c, extra, _arr(getattr(cells, extra), F32))
 
     f = Faces(F, dyn, getattr(faces, "flux_scheme", "upwind"))
     f.pdf = _arr(faces.pdf, F32)

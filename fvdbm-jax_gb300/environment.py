@@ -6,7 +6,9 @@
     for _ in range(n):
         env = env.step()                     # :55-65, returns self
 
-After ``step`` the containers read through to the device: ``cells.pdf`` is
+The environment holds its own copies of the containers (the caller's objects
+are never modified, as with the reference's jitted step).  After ``step``
+``env.cells``/``env.faces``/``env.nodes`` read through to the device: ``cells.pdf`` is
 the updated pdf; ``cells.rho``, ``cells.vel``, ``cells.pdf_eq`` and
 ``faces.pdf`` (the fluxes) are those of the pdf before the last update, as
 the reference leaves them; ``nodes.pdf/rho/vel`` are the node state.
@@ -59,8 +61,9 @@ class Environment:
 
     def __init__(self, cells, faces, nodes, *, ordering: str = "auto", kernel: str = "auto",
                  device: int = 0, finite_volume: bool = False):
-        if not (isinstance(cells, Cells) and isinstance(faces, Faces) and isinstance(nodes, Nodes)):
-            cells, faces, nodes = from_any(cells, faces, nodes)
+        # private copies: like the reference's jitted step, stepping never
+        # modifies the containers the caller passed in
+        cells, faces, nodes = from_any(cells, faces, nodes)
         self.cells, self.faces, self.nodes = cells, faces, nodes
         self.ordering, self.kernel, self.device = ordering, kernel, device
         self.finite_volume = finite_volume
