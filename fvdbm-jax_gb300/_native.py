@@ -47,7 +47,7 @@ class Info(C.Structure):
     _fields_ = [
         ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_nodes", C.c_int32),
         ("n_bc_nodes", C.c_int32), ("n_ghost_faces", C.c_int32), ("kernel", C.c_int32),
-        ("launches_per_step", C.c_int32), ("padded_cells", C.c_int32),
+        ("launches_per_step", C.c_int32), ("padded_cells", C.c_int32), ("const_division", C.c_int32),
         ("bytes_per_step", C.c_double), ("device_bytes", C.c_double),
     ]
 

@@ -1,6 +1,8 @@
 // C ABI of libfvdbm (declared in include/fvdbm.h).
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -46,6 +48,49 @@ struct Handle {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   std::string err;
 };
+
+// Known-divisor division (see cdiv in kernels.cu) is used only for divisors
+// whose exhaustive check on this device found no dividend that it rounds
+// differently from IEEE division; results are cached per device and divisor.
+std::mutex g_cdiv_mu;
+std::map<std::pair<int, uint32_t>, bool> g_cdiv_ok;
+
+cudaError_t make_cdiv(int device, float y, cudaStream_t s, CDiv* out) {
+  const float zr = 1.0f / y;
+  out->y = y;
+  out->zr = zr;
+  out->ok = 0;
+  uint32_t bits;
+  std::memcpy(&bits, &y, 4);
+  const auto key = std::make_pair(device, bits);
+  {
+    std::lock_guard<std::mutex> lk(g_cdiv_mu);
+    auto it = g_cdiv_ok.find(key);
+    if (it != g_cdiv_ok.end()) {
+      out->ok = it->second ? 1 : 0;
+      return cudaSuccess;
+    }
+  }
+  if (!(std::fabs(y) > 0.0f) || !std::isfinite(y) || !std::isfinite(zr)) {
+    std::lock_guard<std::mutex> lk(g_cdiv_mu);
+    g_cdiv_ok[key] = false;
+    return cudaSuccess;
+  }
+  unsigned long long* d_bad = nullptr;
+  unsigned long long bad = ~0ull;
+  cudaError_t e = cudaMalloc(&d_bad, sizeof(bad));
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(d_bad, 0, sizeof(bad), s);
+  if (e == cudaSuccess) e = launch_cdiv_check(y, zr, d_bad, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d_bad);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_cdiv_mu);
+  g_cdiv_ok[key] = (bad == 0);
+  out->ok = (bad == 0) ? 1 : 0;
+  return cudaSuccess;
+}
 
 int fail(Handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
@@ -226,6 +271,10 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   p.c2 = params->c2;
   p.c4x2 = params->c4x2;
   p.c2x2 = params->c2x2;
+  p.finite_n = hp.finite_n ? 1 : 0;
+  CR(make_cdiv(h->device, p.c2, h->stream, &p.d_c2));
+  CR(make_cdiv(h->device, p.c4x2, h->stream, &p.d_c4x2));
+  CR(make_cdiv(h->device, p.c2x2, h->stream, &p.d_c2x2));
 
 #define UP(field, vec)                                                        \
   do {                                                                        \
@@ -495,6 +544,7 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->kernel = h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED;
   info->launches_per_step = (hp.Mc > 0 ? 1 : 0) + (h->fused ? 1 : 2);
   info->padded_cells = hp.Np;
+  info->const_division = (h->dp.d_c2.ok && h->dp.d_c4x2.ok && h->dp.d_c2x2.ok) ? 1 : 0;
   info->bytes_per_step = hp.bytes_per_step;
   info->device_bytes = h->device_bytes;
   return FVDBM_OK;

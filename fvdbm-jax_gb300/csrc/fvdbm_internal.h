@@ -58,7 +58,7 @@ struct HostPlan {
 
   // fused half faces: [K][Np]
   std::vector<int32_t> hf_code;
-  std::vector<float> hf_nx, hf_ny, hf_L, hf_r, hf_D2, hf_scale;
+  std::vector<float> hf_nx, hf_ny, hf_L, hf_r, hf_D2, hf_scale;  // hf_L holds L*sigma
   std::vector<int32_t> gh_a, gh_b;
   std::vector<float> gh_r;
 
@@ -72,6 +72,7 @@ struct HostPlan {
 
   std::vector<float> inv_area;  // [Np] when fv
 
+  bool finite_n = true;
   double bytes_per_step = 0.0;
 };
 
@@ -80,11 +81,21 @@ struct MeshIn;  // fvdbm_mesh_t
 // Build the plan; returns an empty string on success, else the reason.
 std::string build_plan(const void* mesh, const void* params, HostPlan& hp);
 
+// Division by a divisor known in advance: y and zr = RN(1/y).  ok says the
+// three-operation form was verified against IEEE division for every float32
+// dividend on this device (else the kernels divide with '/').
+struct CDiv {
+  float y, zr;
+  int ok;
+};
+
 struct DevPlan {
   int N, Np, F, Fp, K, M, Mp, Mc;
   int scheme, variant, fv;
   int last_cell;
+  int finite_n;  // every face normal is finite (enables the symmetric xi.n form)
   float inv_tau, dt, c2, c4x2, c2x2;
+  CDiv d_c2, d_c4x2, d_c2x2;
   // staged faces
   const int* fs0;
   const int* fs1;
@@ -134,6 +145,9 @@ cudaError_t launch_gather(const DevPlan& p, const float* fin, const float* flux,
                           cudaStream_t s);
 cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
                           cudaStream_t s);
+// Counts the float32 dividends x (all 2^32 bit patterns) for which the
+// known-divisor division differs from x / y; *bad must be zeroed.
+cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, cudaStream_t s);
 cudaError_t launch_scatter_cells(const float* src_aos, float* dst_soa, const int* cell_new, int N,
                                  int Np, cudaStream_t s);
 

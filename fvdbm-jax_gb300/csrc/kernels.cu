@@ -1,14 +1,20 @@
 // FVDBM step kernels for sm_103a (GB300).
 //
-// Every kernel restates the reference's float32 arithmetic operation by
-// operation (MADALERAU/FVDBM-JAX src/dynamics.py, src/containers.py,
-// utils/utils.py): sums are left folds in the reference's index order, the
-// 0*x terms of its integer-lattice dot products are kept, and the library is
-// compiled with --fmad=false so no multiply-add is contracted.  The result is
-// bitwise equal to the CPU oracle.
+// Every kernel restates the reference's float32 arithmetic (MADALERAU/
+// FVDBM-JAX src/dynamics.py, src/containers.py, utils/utils.py) so that the
+// results are bitwise equal to the CPU oracle:
+//   * sums are left folds in the reference's index order;
+//   * the library is compiled with --fmad=false, so no multiply-add is
+//     contracted; the only FMAs are the explicit ones of cdiv();
+//   * rewrites are value-identical: the 0*x terms of the integer-lattice dot
+//     products only matter for non-finite inputs, and such inputs take the
+//     literal (faithful) path; the +-symmetric lattice directions reuse one
+//     quotient (RN(-a/c) == -RN(a/c)).
 //
 // Layout: cell pdfs are SoA [9][Np] float32 in device (renumbered) cell
 // order; node state is SoA [9][Mp]; per-cell face slots are SoA [K][Np].
+#include <cfloat>
+
 #include "fvdbm_internal.h"
 
 namespace fvdbm {
@@ -17,18 +23,34 @@ __constant__ float c_W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1
                              (float)(1.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 36.0),
                              (float)(1.0 / 36.0), (float)(1.0 / 36.0), (float)(1.0 / 36.0)};
 
-// rho = sum_q f_q; u = (KSI^T f) / rho   (src/dynamics.py:35-47)
-__device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, float& uy) {
-  float r = f[0] + f[1];
-  r = r + f[2];
-  r = r + f[3];
-  r = r + f[4];
-  r = r + f[5];
-  r = r + f[6];
-  r = r + f[7];
-  r = r + f[8];
-  // KSI x column: 0 1 0 -1 0 1 -1 -1 1
-  float mx = 0.0f * f[0];
+__device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
+
+// Correctly rounded x/y for a divisor known in advance, after Brisebarre,
+// Muller and Raina, "Accelerating correctly rounded floating-point division
+// when the divisor is known in advance", IEEE Trans. Computers 53(8), 2004:
+// with zr = RN(1/y), q = RN(x*zr), r = RN(x - q*y) (exact through an FMA),
+// q' = RN(q + r*zr).  Quotients outside the normal range take x/y.  Whether
+// this equals x/y for every float32 x is checked exhaustively on the device
+// (k_cdiv_check) before the kernels are allowed to use it.
+__device__ __forceinline__ float cdiv_fast(float x, float y, float zr) {
+  const float q = __fmul_rn(x, zr);
+  const float r = __fmaf_rn(-q, y, x);
+  return __fmaf_rn(r, zr, q);
+}
+
+__device__ __forceinline__ float cdiv(float x, const CDiv& d) {
+  if (d.ok) {
+    const float q = cdiv_fast(x, d.y, d.zr);
+    const float a = fabsf(q);
+    if ((a >= FLT_MIN && a <= FLT_MAX) || x == 0.0f) return q;
+  }
+  return x / d.y;
+}
+
+// ---------------------------------------------------------------------------
+// Literal forms (src/dynamics.py:35-47,70-74), used for non-finite inputs.
+__device__ __forceinline__ void macros_literal(const float f[Q], float& mx, float& my) {
+  mx = 0.0f * f[0];
   mx = mx + f[1];
   mx = mx + 0.0f * f[2];
   mx = mx + (-f[3]);
@@ -37,8 +59,7 @@ __device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, 
   mx = mx + (-f[6]);
   mx = mx + (-f[7]);
   mx = mx + f[8];
-  // KSI y column: 0 0 1 0 -1 1 1 -1 -1
-  float my = 0.0f * f[0];
+  my = 0.0f * f[0];
   my = my + 0.0f * f[1];
   my = my + f[2];
   my = my + 0.0f * f[3];
@@ -47,13 +68,10 @@ __device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, 
   my = my + f[6];
   my = my + (-f[7]);
   my = my + (-f[8]);
-  rho = r;
-  ux = mx / r;
-  uy = my / r;
 }
 
-// xi_q . (x, y) folded over the two components (src/dynamics.py:72)
-__device__ __forceinline__ void xi_dot(float x, float y, float a[Q]) {
+// xi_q . (x, y) folded over the two components, 0*x terms kept
+__device__ __forceinline__ void xi_dot_literal(float x, float y, float a[Q]) {
   const float zx = 0.0f * x, zy = 0.0f * y;
   a[0] = zx + zy;
   a[1] = x + zy;
@@ -66,104 +84,190 @@ __device__ __forceinline__ void xi_dot(float x, float y, float a[Q]) {
   a[8] = x + (-y);
 }
 
-// feq = (W*rho) * (((1 + a/C^2) + a^2/(2C^4)) - u.u/(2C^2))  (src/dynamics.py:70-74)
-__device__ __forceinline__ void feq9(float rho, float ux, float uy, float c2, float c4x2,
-                                     float c2x2, float out[Q]) {
+__device__ __forceinline__ void feq9_literal(float rho, float ux, float uy, const DevPlan& p,
+                                          float out[Q]) {
   float a[Q];
-  xi_dot(ux, uy, a);
+  xi_dot_literal(ux, uy, a);
   const float uu = ux * ux + uy * uy;
-  const float t = uu / c2x2;
-#pragma unroll
+  const float t = uu / p.c2x2;
   for (int q = 0; q < Q; ++q) {
-    float s = 1.0f + a[q] / c2;
-    s = s + (a[q] * a[q]) / c4x2;
+    float s = 1.0f + a[q] / p.c2;
+    s = s + (a[q] * a[q]) / p.c4x2;
     s = s - t;
     out[q] = (c_W[q] * rho) * s;
   }
 }
 
-// Face flux from the pdfs on the slot-0 (left) and slot-1 (right) sides
-// (src/containers.py:215-278, src/faces.py:54-74,119-141).
-template <int SCHEME, int VARIANT>
-__device__ __forceinline__ void face_flux(const float lf[Q], const float rf[Q], float nx, float ny,
-                                          float L, float r, float D2, float dt, float scale,
-                                          const float* qscale, int qstride, float out[Q]) {
-  float v[Q];
-  xi_dot(nx, ny, v);
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    float phi;
-    if (SCHEME == 0) {
-      phi = v[q] >= 0.0f ? lf[q] : rf[q];
-    } else {
-      const float interp = r - (v[q] * dt) / D2;
-      phi = lf[q] + (rf[q] - lf[q]) * interp;
-    }
-    float fl = (phi * v[q]) * L;
-    if (VARIANT == 1) fl = fl * scale;
-    if (VARIANT == 2) fl = fl * qscale[q * qstride];
-    out[q] = fl;
+// rho = sum_q f_q; u = (KSI^T f)/rho.  For finite rho every f_q is finite and
+// the 0*f_q terms of the literal fold are +-0, which leave the sum unchanged.
+__device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, float& uy) {
+  float r = f[0] + f[1];
+  r = r + f[2];
+  r = r + f[3];
+  r = r + f[4];
+  r = r + f[5];
+  r = r + f[6];
+  r = r + f[7];
+  r = r + f[8];
+  float mx, my;
+  if (finite(r)) {
+    mx = ((((f[1] - f[3]) + f[5]) - f[6]) - f[7]) + f[8];
+    my = ((((f[2] - f[4]) + f[5]) + f[6]) - f[7]) - f[8];
+  } else {
+    macros_literal(f, mx, my);
   }
+  rho = r;
+  ux = mx / r;
+  uy = my / r;
+}
+
+// feq_q = (W_q rho) * (((1 + a_q/C^2) + a_q^2/(2C^4)) - u.u/(2C^2)).
+// With finite u: a_3 = -a_1, a_4 = -a_2, a_7 = -a_5, a_8 = -a_6 exactly, and
+// a_0 = +-0 gives s_0 = 1 - u.u/(2C^2).
+__device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPlan& p, float out[Q]) {
+  if (!(finite(ux) && finite(uy))) {
+    feq9_literal(rho, ux, uy, p, out);
+    return;
+  }
+  const float uu = ux * ux + uy * uy;
+  const float t = cdiv(uu, p.d_c2x2);
+  const float a5 = ux + uy, a6 = uy - ux;
+  const float x1 = cdiv(ux, p.d_c2), y1 = cdiv(ux * ux, p.d_c4x2);
+  const float x2 = cdiv(uy, p.d_c2), y2 = cdiv(uy * uy, p.d_c4x2);
+  const float x5 = cdiv(a5, p.d_c2), y5 = cdiv(a5 * a5, p.d_c4x2);
+  const float x6 = cdiv(a6, p.d_c2), y6 = cdiv(a6 * a6, p.d_c4x2);
+  float s[Q];
+  s[0] = 1.0f - t;
+  s[1] = ((1.0f + x1) + y1) - t;
+  s[3] = ((1.0f - x1) + y1) - t;
+  s[2] = ((1.0f + x2) + y2) - t;
+  s[4] = ((1.0f - x2) + y2) - t;
+  s[5] = ((1.0f + x5) + y5) - t;
+  s[7] = ((1.0f - x5) + y5) - t;
+  s[6] = ((1.0f + x6) + y6) - t;
+  s[8] = ((1.0f - x6) + y6) - t;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) out[q] = (c_W[q] * rho) * s[q];
+}
+
+// v_q = xi_q . n (src/containers.py:235); symmetric form for finite n
+__device__ __forceinline__ void xi_dot_n(float nx, float ny, bool finite_n, float v[Q]) {
+  if (!finite_n) {
+    xi_dot_literal(nx, ny, v);
+    return;
+  }
+  const float s = nx + ny, d = ny - nx;
+  v[0] = 0.0f;
+  v[1] = nx;
+  v[2] = ny;
+  v[3] = -nx;
+  v[4] = -ny;
+  v[5] = s;
+  v[6] = d;
+  v[7] = -s;
+  v[8] = -d;
+}
+
+// Lax-Wendroff weights interp_q = d0/(d0+d1) - (v_q*dt)/(2(d0+d1))
+// (src/containers.py:274); (-v*dt)/D2 == -((v*dt)/D2).
+__device__ __forceinline__ void lw_interp(const float v[Q], float r, float D2, float dt,
+                                          bool finite_n, float w[Q]) {
+  if (!finite_n) {
+    for (int q = 0; q < Q; ++q) w[q] = r - (v[q] * dt) / D2;
+    return;
+  }
+  const float t1 = (v[1] * dt) / D2, t2 = (v[2] * dt) / D2;
+  const float t5 = (v[5] * dt) / D2, t6 = (v[6] * dt) / D2;
+  w[0] = r - (v[0] * dt) / D2;
+  w[1] = r - t1;
+  w[3] = r + t1;
+  w[2] = r - t2;
+  w[4] = r + t2;
+  w[5] = r - t5;
+  w[7] = r + t5;
+  w[6] = r - t6;
+  w[8] = r + t6;
 }
 
 // ---------------------------------------------------------------------------
-// Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  Velocity
-// nodes (type 1) take rho = IDW(cell rho); density nodes (type 2) take
-// u = IDW(cell u); both set pdf = feq(rho,u) + IDW(f - feq).  Cell macros are
-// recomputed from f with the same arithmetic as the cell kernels.
+// Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  One group of
+// 8 lanes per node: each lane evaluates one of the node's cells (macros, feq,
+// the IDW products), then every lane folds the products in the reference's
+// entry order through shuffles.  Velocity nodes (type 1) take rho =
+// IDW(cell rho); density nodes (type 2) take u = IDW(cell u); both set pdf =
+// feq(rho, u) + IDW(f - feq).
+constexpr int NODE_LANES = 8;
+
 __global__ void __launch_bounds__(128) k_nodes(DevPlan p, const float* __restrict__ f) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= p.Mc) return;
-  const int type = p.nd_type[m];
-  const int b = p.nd_ptr[m], e = p.nd_ptr[m + 1];
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = tid / NODE_LANES;
+  const int lane = threadIdx.x % NODE_LANES;
+  if (m >= p.Mc) return;  // whole 8-lane group leaves together
+  const unsigned mask = 0xFFu << (threadIdx.x & 24);
+  const int b = __ldg(p.nd_ptr + m), e = __ldg(p.nd_ptr + m + 1);
+  const size_t Np = p.Np;
   float ar = 0.0f, ax = 0.0f, ay = 0.0f, an[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) an[q] = 0.0f;
   bool first = true;
-  for (int j = b; j < e; ++j) {
-    const unsigned code = p.nd_cell[j];
-    const int c = int(code & ~ND_NEQ_ZERO);
-    const float w = p.nd_w[j];
-    float fc[Q], eq[Q];
+  for (int base = b; base < e; base += NODE_LANES) {
+    const int j = base + lane;
+    float xr = 0.0f, xx = 0.0f, xy = 0.0f, xn[Q];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) fc[q] = __ldg(f + size_t(q) * p.Np + c);
-    float rho, ux, uy;
-    macros(fc, rho, ux, uy);
-    feq9(rho, ux, uy, p.c2, p.c4x2, p.c2x2, eq);
-    const bool zero = (code & ND_NEQ_ZERO) != 0;
-    if (first) {
-      ar = rho * w;
-      ax = ux * w;
-      ay = uy * w;
+    for (int q = 0; q < Q; ++q) xn[q] = 0.0f;
+    if (j < e) {
+      const unsigned code = __ldg(p.nd_cell + j);
+      const int c = int(code & ~ND_NEQ_ZERO);
+      const float w = __ldg(p.nd_w + j);
+      float fc[Q], eq[Q];
 #pragma unroll
-      for (int q = 0; q < Q; ++q) an[q] = (zero ? 0.0f : fc[q] - eq[q]) * w;
+      for (int q = 0; q < Q; ++q) fc[q] = __ldg(f + q * Np + c);
+      float rho, ux, uy;
+      macros(fc, rho, ux, uy);
+      feq9(rho, ux, uy, p, eq);
+      const bool zero = (code & ND_NEQ_ZERO) != 0;
+      xr = rho * w;
+      xx = ux * w;
+      xy = uy * w;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) xn[q] = (zero ? 0.0f : fc[q] - eq[q]) * w;
+    }
+    const int cnt = min(NODE_LANES, e - base);
+    for (int t = 0; t < cnt; ++t) {
+      const float vr = __shfl_sync(mask, xr, t, NODE_LANES);
+      const float vx = __shfl_sync(mask, xx, t, NODE_LANES);
+      const float vy = __shfl_sync(mask, xy, t, NODE_LANES);
+      if (first) {
+        ar = vr;
+        ax = vx;
+        ay = vy;
+      } else {
+        ar = ar + vr;
+        ax = ax + vx;
+        ay = ay + vy;
+      }
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const float vn = __shfl_sync(mask, xn[q], t, NODE_LANES);
+        an[q] = first ? vn : an[q] + vn;
+      }
       first = false;
-    } else {
-      ar = ar + rho * w;
-      ax = ax + ux * w;
-      ay = ay + uy * w;
-#pragma unroll
-      for (int q = 0; q < Q; ++q) an[q] = an[q] + (zero ? 0.0f : fc[q] - eq[q]) * w;
     }
   }
-  if (p.nd_npad[m] > 0) {
+  if (__ldg(p.nd_npad + m) > 0) {
     // padded (-1, weight 0) entries gather the last cell: rho*0, u*0
     float fc[Q];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) fc[q] = __ldg(f + size_t(q) * p.Np + p.last_cell);
+    for (int q = 0; q < Q; ++q) fc[q] = __ldg(f + q * Np + p.last_cell);
     float rho, ux, uy;
     macros(fc, rho, ux, uy);
-    if (first) {
-      ar = rho * 0.0f;
-      ax = ux * 0.0f;
-      ay = uy * 0.0f;
-    } else {
-      ar = ar + rho * 0.0f;
-      ax = ax + ux * 0.0f;
-      ay = ay + uy * 0.0f;
-    }
+    ar = first ? rho * 0.0f : ar + rho * 0.0f;
+    ax = first ? ux * 0.0f : ax + ux * 0.0f;
+    ay = first ? uy * 0.0f : ay + uy * 0.0f;
   }
-  const float sw = p.nd_sumw[m];
+  if (lane != 0) return;
+  const float sw = __ldg(p.nd_sumw + m);
+  const int type = __ldg(p.nd_type + m);
   float rho_p, ux_p, uy_p;
   if (type == 1) {
     rho_p = ar / sw;
@@ -178,7 +282,7 @@ __global__ void __launch_bounds__(128) k_nodes(DevPlan p, const float* __restric
     p.node_vel[p.Mp + m] = uy_p;
   }
   float eqn[Q];
-  feq9(rho_p, ux_p, uy_p, p.c2, p.c4x2, p.c2x2, eqn);
+  feq9(rho_p, ux_p, uy_p, p, eqn);
 #pragma unroll
   for (int q = 0; q < Q; ++q) p.node_pdf[size_t(q) * p.Mp + m] = eqn[q] + an[q] / sw;
 }
@@ -188,7 +292,53 @@ __global__ void __launch_bounds__(128) k_nodes(DevPlan p, const float* __restric
 // (recomputed from the canonical slot-0/slot-1 pair, so both neighbours get
 // bit-identical fluxes without a flux array or atomics), the signed flux sum
 // and the BGK/explicit-Euler update (src/containers.py:107-121).
-template <int SCHEME, int VARIANT, bool FV>
+template <int SCHEME, int VARIANT, bool FIRST>
+__device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin, size_t Np,
+                                           int i, int k, const float f[Q], float acc[Q]) {
+  const size_t s = size_t(k) * Np + i;
+  const int code = __ldg(p.hf_code + s);
+  const float nx = __ldg(p.hf_nx + s), ny = __ldg(p.hf_ny + s);
+  const float Ls = __ldg(p.hf_L + s);  // L * sigma
+  const int other = code >> HF_SHIFT;
+  const bool slot1 = (code & HF_SLOT1) != 0;
+  float o[Q];
+  if (code & HF_GHOST) {
+    // ghost = m + (m - f_known)*(d_ghost/d_known), m = mean of the face's two
+    // end-node pdfs (src/containers.py:280-287, utils/utils.py:153)
+    const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
+    const float rg = __ldg(p.gh_r + other);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const float mq = (__ldg(p.node_pdf + size_t(q) * p.Mp + a) +
+                        __ldg(p.node_pdf + size_t(q) * p.Mp + b)) / 2.0f;
+      o[q] = mq + (mq - f[q]) * rg;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) o[q] = __ldg(fin + q * Np + other);
+  }
+  float v[Q];
+  xi_dot_n(nx, ny, p.finite_n != 0, v);
+  float w[Q];
+  if (SCHEME == 1) lw_interp(v, __ldg(p.hf_r + s), __ldg(p.hf_D2 + s), p.dt, p.finite_n != 0, w);
+  const float scale = (VARIANT == 1) ? __ldg(p.hf_scale + s) : 1.0f;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    float phi;
+    if (SCHEME == 0) {
+      // upwind: slot 0 when xi.n >= 0, else slot 1
+      phi = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
+    } else {
+      const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
+      phi = lq + (rq - lq) * w[q];
+    }
+    float x = (phi * v[q]) * Ls;
+    if (VARIANT == 1) x = x * scale;
+    acc[q] = FIRST ? x : acc[q] + x;
+  }
+}
+
+template <int SCHEME, int VARIANT, bool FV, int KT>
 __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restrict__ fin,
                                                float* __restrict__ fout) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -199,52 +349,21 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
   for (int q = 0; q < Q; ++q) f[q] = __ldg(fin + q * Np + i);
   float rho, ux, uy, eq[Q];
   macros(f, rho, ux, uy);
-  feq9(rho, ux, uy, p.c2, p.c4x2, p.c2x2, eq);
+  feq9(rho, ux, uy, p, eq);
 
   float acc[Q];
-  for (int k = 0; k < p.K; ++k) {
-    const size_t s = k * Np + i;
-    const int code = __ldg(p.hf_code + s);
-    const float nx = __ldg(p.hf_nx + s), ny = __ldg(p.hf_ny + s), L = __ldg(p.hf_L + s);
-    float r = 0.0f, D2 = 1.0f, scale = 1.0f;
-    if (SCHEME == 1) {
-      r = __ldg(p.hf_r + s);
-      D2 = __ldg(p.hf_D2 + s);
-    }
-    if (VARIANT == 1) scale = __ldg(p.hf_scale + s);
-    const int other = code >> HF_SHIFT;
-    float o[Q];
-    if (code & HF_GHOST) {
-      // ghost = m + (m - f_known)*(d_ghost/d_known), m = mean of the face's
-      // two end-node pdfs (src/containers.py:280-287, utils/utils.py:153)
-      const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
-      const float rg = __ldg(p.gh_r + other);
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const float mq = (p.node_pdf[size_t(q) * p.Mp + a] + p.node_pdf[size_t(q) * p.Mp + b]) / 2.0f;
-        o[q] = mq + (mq - f[q]) * rg;
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < Q; ++q) o[q] = __ldg(fin + q * Np + other);
-    }
-    float fl[Q];
-    if (code & HF_SLOT1)
-      face_flux<SCHEME, VARIANT>(o, f, nx, ny, L, r, D2, p.dt, scale, nullptr, 0, fl);
-    else
-      face_flux<SCHEME, VARIANT>(f, o, nx, ny, L, r, D2, p.dt, scale, nullptr, 0, fl);
-    const float sg = float((code & 3) - 1);
-    if (k == 0) {
-#pragma unroll
-      for (int q = 0; q < Q; ++q) acc[q] = fl[q] * sg;
-    } else {
-#pragma unroll
-      for (int q = 0; q < Q; ++q) acc[q] = acc[q] + fl[q] * sg;
-    }
-  }
-  if (p.K == 0) {
+  const int K = KT > 0 ? KT : p.K;
+  if (K == 0) {
 #pragma unroll
     for (int q = 0; q < Q; ++q) acc[q] = 0.0f;
+  } else {
+    fused_face<SCHEME, VARIANT, true>(p, fin, Np, i, 0, f, acc);
+    if (KT > 0) {
+#pragma unroll
+      for (int k = 1; k < KT; ++k) fused_face<SCHEME, VARIANT, false>(p, fin, Np, i, k, f, acc);
+    } else {
+      for (int k = 1; k < K; ++k) fused_face<SCHEME, VARIANT, false>(p, fin, Np, i, k, f, acc);
+    }
   }
   if (FV) {
     const float ia = __ldg(p.inv_area + i);
@@ -297,17 +416,19 @@ __global__ void __launch_bounds__(256) k_face(DevPlan p, const float* __restrict
       for (int q = 0; q < Q; ++q) rf[q] = mq[q] + (mq[q] - __ldg(f + q * Np + kn)) * rg;
     }
   }
-  float r = 0.0f, D2 = 1.0f, scale = 1.0f;
-  if (SCHEME == 1) {
-    r = p.fr[j];
-    D2 = p.fD2[j];
-  }
-  if (VARIANT == 1) scale = p.fscale[j];
-  float fl[Q];
-  face_flux<SCHEME, VARIANT>(lf, rf, p.fnx[j], p.fny[j], p.fL[j], r, D2, p.dt, scale,
-                             VARIANT == 2 ? p.fscale + j : nullptr, p.Fp, fl);
+  float v[Q], w[Q];
+  xi_dot_n(p.fnx[j], p.fny[j], p.finite_n != 0, v);
+  if (SCHEME == 1) lw_interp(v, p.fr[j], p.fD2[j], p.dt, p.finite_n != 0, w);
+  const float L = p.fL[j];
+  const float scale = (VARIANT == 1) ? p.fscale[j] : 1.0f;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) flux[size_t(q) * p.Fp + j] = fl[q];
+  for (int q = 0; q < Q; ++q) {
+    const float phi = (SCHEME == 0) ? (v[q] >= 0.0f ? lf[q] : rf[q]) : lf[q] + (rf[q] - lf[q]) * w[q];
+    float x = (phi * v[q]) * L;
+    if (VARIANT == 1) x = x * scale;
+    if (VARIANT == 2) x = x * p.fscale[size_t(q) * p.Fp + j];
+    flux[size_t(q) * p.Fp + j] = x;
+  }
 }
 
 // Staged form, kernel 3: cell-centric gather of the signed face fluxes over
@@ -324,19 +445,17 @@ __global__ void __launch_bounds__(256) k_gather(DevPlan p, const float* __restri
   for (int q = 0; q < Q; ++q) f[q] = __ldg(fin + q * Np + i);
   float rho, ux, uy, eq[Q];
   macros(f, rho, ux, uy);
-  feq9(rho, ux, uy, p.c2, p.c4x2, p.c2x2, eq);
+  feq9(rho, ux, uy, p, eq);
   float acc[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) acc[q] = 0.0f;
   for (int k = 0; k < p.K; ++k) {
     const int fi = __ldg(p.cf_face + k * Np + i);
     const float sg = __ldg(p.cf_sign + k * Np + i);
-    if (k == 0) {
 #pragma unroll
-      for (int q = 0; q < Q; ++q) acc[q] = __ldg(flux + size_t(q) * p.Fp + fi) * sg;
-    } else {
-#pragma unroll
-      for (int q = 0; q < Q; ++q) acc[q] = acc[q] + __ldg(flux + size_t(q) * p.Fp + fi) * sg;
+    for (int q = 0; q < Q; ++q) {
+      const float x = __ldg(flux + size_t(q) * p.Fp + fi) * sg;
+      acc[q] = (k == 0) ? x : acc[q] + x;
     }
   }
   if (FV) {
@@ -361,7 +480,7 @@ __global__ void __launch_bounds__(256) k_macros(DevPlan p, const float* __restri
   for (int q = 0; q < Q; ++q) fc[q] = f[q * Np + i];
   float rho, ux, uy;
   macros(fc, rho, ux, uy);
-  feq9(rho, ux, uy, p.c2, p.c4x2, p.c2x2, eq);
+  feq9(rho, ux, uy, p, eq);
   rho_o[i] = rho;
   vel_o[i] = ux;
   vel_o[Np + i] = uy;
@@ -379,29 +498,51 @@ __global__ void k_aos_to_soa(const float* __restrict__ src, float* __restrict__ 
   for (int q = 0; q < Q; ++q) dst[size_t(q) * Np + d] = src[size_t(c) * Q + q];
 }
 
+// Exhaustive check of cdiv against IEEE division: every float32 bit pattern
+// as dividend; counts the dividends whose quotients differ in value (NaN
+// matches NaN).  Not on the step path; runs once per divisor per process.
+__global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, unsigned long long* bad) {
+  const CDiv d{y, zr, 1};
+  unsigned long long local = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+       u < (1ull << 32); u += stride) {
+    const float x = __uint_as_float(unsigned(u));
+    const float a = cdiv(x, d);
+    const float b = x / y;
+    if (!(a == b || (a != a && b != b))) ++local;
+  }
+  for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xFFFFFFFFu, local, off);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
+}
+
 // ---------------------------------------------------------------------------
-static inline int blocks(int n, int t) { return (n + t - 1) / t; }
+static inline int blocks(long long n, int t) { return int((n + t - 1) / t); }
 
 cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s) {
   if (p.Mc == 0) return cudaSuccess;
-  k_nodes<<<blocks(p.Mc, 128), 128, 0, s>>>(p, f);
+  k_nodes<<<blocks((long long)p.Mc * NODE_LANES, 128), 128, 0, s>>>(p, f);
   return cudaGetLastError();
 }
 
 template <int S, int V>
-static void fused_dispatch_fv(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
-  if (p.fv)
-    k_fused<S, V, true><<<blocks(p.N, 256), 256, 0, s>>>(p, fin, fout);
-  else
-    k_fused<S, V, false><<<blocks(p.N, 256), 256, 0, s>>>(p, fin, fout);
+static void fused_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
+  const int g = blocks(p.N, 256);
+  if (p.K == 3) {
+    if (p.fv) k_fused<S, V, true, 3><<<g, 256, 0, s>>>(p, fin, fout);
+    else k_fused<S, V, false, 3><<<g, 256, 0, s>>>(p, fin, fout);
+  } else {
+    if (p.fv) k_fused<S, V, true, 0><<<g, 256, 0, s>>>(p, fin, fout);
+    else k_fused<S, V, false, 0><<<g, 256, 0, s>>>(p, fin, fout);
+  }
 }
 
 cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
   if (p.N == 0) return cudaSuccess;
-  if (p.scheme == 0 && p.variant == 0) fused_dispatch_fv<0, 0>(p, fin, fout, s);
-  else if (p.scheme == 1 && p.variant == 0) fused_dispatch_fv<1, 0>(p, fin, fout, s);
-  else if (p.scheme == 0 && p.variant == 1) fused_dispatch_fv<0, 1>(p, fin, fout, s);
-  else if (p.scheme == 1 && p.variant == 1) fused_dispatch_fv<1, 1>(p, fin, fout, s);
+  if (p.scheme == 0 && p.variant == 0) fused_dispatch<0, 0>(p, fin, fout, s);
+  else if (p.scheme == 1 && p.variant == 0) fused_dispatch<1, 0>(p, fin, fout, s);
+  else if (p.scheme == 0 && p.variant == 1) fused_dispatch<0, 1>(p, fin, fout, s);
+  else if (p.scheme == 1 && p.variant == 1) fused_dispatch<1, 1>(p, fin, fout, s);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
@@ -433,6 +574,14 @@ cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* v
                           cudaStream_t s) {
   if (p.N == 0) return cudaSuccess;
   k_macros<<<blocks(p.N, 256), 256, 0, s>>>(p, f, rho, vel, feq);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_cdiv_check<<<sms * 8, 256, 0, s>>>(y, zr, bad);
   return cudaGetLastError();
 }
 

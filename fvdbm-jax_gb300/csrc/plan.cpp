@@ -322,6 +322,7 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     hp.fs1[j] = cnew(s1);
     hp.fnx[j] = m.face_n[2 * f];
     hp.fny[j] = m.face_n[2 * f + 1];
+    if (!std::isfinite(hp.fnx[j]) || !std::isfinite(hp.fny[j])) hp.finite_n = false;
     hp.fL[j] = m.face_L[f];
     const float D = d0 + d1;
     hp.fr[j] = d0 / D;
@@ -389,7 +390,8 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       hp.hf_code[s] = code;
       hp.hf_nx[s] = hp.fnx[j];
       hp.hf_ny[s] = hp.fny[j];
-      hp.hf_L[s] = hp.fL[j];
+      // ((phi*v)*L)*sigma == (phi*v)*(L*sigma) exactly for sigma in {-1,0,1}
+      hp.hf_L[s] = hp.fL[j] * float(sg);
       if (pr.flux_scheme == FVDBM_LAX_WENDROFF) {
         hp.hf_r[s] = hp.fr[j];
         hp.hf_D2[s] = hp.fD2[j];

@@ -108,6 +108,9 @@ typedef struct fvdbm_info {
   int32_t kernel;           /* family actually used */
   int32_t launches_per_step;
   int32_t padded_cells;     /* row stride of the [9][Np] pdf */
+  int32_t const_division;   /* 1: divisions by the lattice constants use the
+                               known-divisor form, verified on this device to
+                               equal IEEE division for every float32 dividend */
   double bytes_per_step;    /* algorithmic bytes of one step */
   double device_bytes;      /* device memory held by the handle */
 } fvdbm_info_t;

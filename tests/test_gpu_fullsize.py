@@ -129,3 +129,13 @@ def test_state_round_trip_and_midrun_write():
     st["nodes_vel"] = v
     st = OC.step(geo, st, dyn.inv_tau, dyn.dt32, n_steps=2)
     _compare(env, st)
+
+
+def test_known_divisor_division_verified_and_used():
+    """The three lattice-constant divisors pass the exhaustive check (every
+    float32 dividend gives the IEEE quotient), so the kernels use it."""
+    from fvdbm_jax_gb300 import Environment, meshgen
+    m, dyn, c, f, n = _case(meshgen.cavity(n=5))
+    env = Environment(c, f, n)
+    env.init()
+    assert env.info()["const_division"] == 1
