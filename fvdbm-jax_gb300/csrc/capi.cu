@@ -55,6 +55,24 @@ struct Handle {
 std::mutex g_cdiv_mu;
 std::map<std::pair<int, uint32_t>, bool> g_cdiv_ok;
 
+cudaError_t run_cdiv_check(float y, float zr, cudaStream_t s, unsigned long long* bad,
+                           unsigned* example) {
+  unsigned long long* d_bad = nullptr;
+  unsigned* d_ex = nullptr;
+  cudaError_t e = cudaMalloc(&d_bad, sizeof(unsigned long long));
+  if (e != cudaSuccess) return e;
+  e = cudaMalloc(&d_ex, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_ex, 0xFF, sizeof(unsigned), s);
+  if (e == cudaSuccess) e = launch_cdiv_check(y, zr, d_bad, d_ex, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(example, d_ex, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d_bad);
+  if (d_ex) cudaFree(d_ex);
+  return e;
+}
+
 cudaError_t make_cdiv(int device, float y, cudaStream_t s, CDiv* out) {
   const float zr = 1.0f / y;
   out->y = y;
@@ -76,15 +94,9 @@ cudaError_t make_cdiv(int device, float y, cudaStream_t s, CDiv* out) {
     g_cdiv_ok[key] = false;
     return cudaSuccess;
   }
-  unsigned long long* d_bad = nullptr;
   unsigned long long bad = ~0ull;
-  cudaError_t e = cudaMalloc(&d_bad, sizeof(bad));
-  if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(d_bad, 0, sizeof(bad), s);
-  if (e == cudaSuccess) e = launch_cdiv_check(y, zr, d_bad, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(d_bad);
+  unsigned example = 0;
+  cudaError_t e = run_cdiv_check(y, zr, s, &bad, &example);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lk(g_cdiv_mu);
   g_cdiv_ok[key] = (bad == 0);
@@ -400,6 +412,26 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   int rc = enqueue_steps(h, n);
   if (rc != FVDBM_OK) return rc;
   h->steps_done += n_steps;
+  return FVDBM_OK;
+}
+
+int fvdbm_const_div_check(int32_t device, float divisor, uint64_t* mismatches,
+                          uint32_t* first_mismatch) {
+  if (!mismatches || !first_mismatch) return FVDBM_EINVAL;
+  cudaError_t e = cudaSetDevice(device);
+  cudaStream_t s = nullptr;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  unsigned long long bad = 0;
+  unsigned ex = 0xFFFFFFFFu;
+  if (e == cudaSuccess) e = run_cdiv_check(divisor, 1.0f / divisor, s, &bad, &ex);
+  if (s) cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = std::string("fvdbm_const_div_check: ") + cudaGetErrorString(e);
+    return FVDBM_ECUDA;
+  }
+  *mismatches = bad;
+  *first_mismatch = ex;
   return FVDBM_OK;
 }
 

@@ -146,8 +146,10 @@ cudaError_t launch_gather(const DevPlan& p, const float* fin, const float* flux,
 cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
                           cudaStream_t s);
 // Counts the float32 dividends x (all 2^32 bit patterns) for which the
-// known-divisor division differs from x / y; *bad must be zeroed.
-cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, cudaStream_t s);
+// known-divisor division differs from x / y, and the lowest such bit pattern;
+// *bad must be zeroed and *example set to 0xFFFFFFFF.
+cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsigned* example,
+                              cudaStream_t s);
 cudaError_t launch_scatter_cells(const float* src_aos, float* dst_soa, const int* cell_new, int N,
                                  int Np, cudaStream_t s);
 

@@ -25,24 +25,32 @@ __constant__ float c_W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1
 
 __device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
 
-// Correctly rounded x/y for a divisor known in advance, after Brisebarre,
-// Muller and Raina, "Accelerating correctly rounded floating-point division
-// when the divisor is known in advance", IEEE Trans. Computers 53(8), 2004:
-// with zr = RN(1/y), q = RN(x*zr), r = RN(x - q*y) (exact through an FMA),
-// q' = RN(q + r*zr).  Quotients outside the normal range take x/y.  Whether
-// this equals x/y for every float32 x is checked exhaustively on the device
-// (k_cdiv_check) before the kernels are allowed to use it.
+// Correctly rounded x/y for a divisor known in advance.  With zr = RN(1/y):
+// q0 = RN(x*zr) is within 1.5 ulp of x/y; one correction
+// q1 = RN(q0 + RN(x - q0*y)*zr) (remainder exact through an FMA) makes it
+// faithful; by Markstein's theorem (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990) a second correction q2 = RN(q1 + (x - q1*y)*zr) is then the correctly
+// rounded quotient (Brisebarre, Muller and Raina, IEEE Trans. Computers 53(8),
+// 2004, show that the first correction alone fails for some divisors).
+// Whether this equals x/y for every float32 x is checked exhaustively on the
+// device (k_cdiv_check) before the kernels are allowed to use it.
 __device__ __forceinline__ float cdiv_fast(float x, float y, float zr) {
-  const float q = __fmul_rn(x, zr);
-  const float r = __fmaf_rn(-q, y, x);
-  return __fmaf_rn(r, zr, q);
+  const float q0 = __fmul_rn(x, zr);
+  const float r0 = __fmaf_rn(-q0, y, x);
+  const float q1 = __fmaf_rn(r0, zr, q0);
+  const float r1 = __fmaf_rn(-q1, y, x);
+  return __fmaf_rn(r1, zr, q1);
 }
 
+// The remainders are exact only while they stay above the subnormal range,
+// so tiny dividends (|x| < 2^-100) and quotients outside the normal range
+// take x/y; x == 0 gives +-0 either way.
 __device__ __forceinline__ float cdiv(float x, const CDiv& d) {
   if (d.ok) {
     const float q = cdiv_fast(x, d.y, d.zr);
     const float a = fabsf(q);
-    if ((a >= FLT_MIN && a <= FLT_MAX) || x == 0.0f) return q;
+    if ((fabsf(x) >= 0x1p-100f && a >= FLT_MIN && a <= FLT_MAX) || x == 0.0f) return q;
   }
   return x / d.y;
 }
@@ -501,19 +509,30 @@ __global__ void k_aos_to_soa(const float* __restrict__ src, float* __restrict__ 
 // Exhaustive check of cdiv against IEEE division: every float32 bit pattern
 // as dividend; counts the dividends whose quotients differ in value (NaN
 // matches NaN).  Not on the step path; runs once per divisor per process.
-__global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, unsigned long long* bad) {
+__global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, unsigned long long* bad,
+                                                    unsigned* example) {
   const CDiv d{y, zr, 1};
   unsigned long long local = 0;
+  unsigned ex = 0xFFFFFFFFu;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
        u < (1ull << 32); u += stride) {
     const float x = __uint_as_float(unsigned(u));
     const float a = cdiv(x, d);
     const float b = x / y;
-    if (!(a == b || (a != a && b != b))) ++local;
+    if (!(a == b || (a != a && b != b))) {
+      ++local;
+      ex = min(ex, unsigned(u));
+    }
   }
-  for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xFFFFFFFFu, local, off);
-  if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
+  for (int off = 16; off > 0; off >>= 1) {
+    local += __shfl_down_sync(0xFFFFFFFFu, local, off);
+    ex = min(ex, __shfl_down_sync(0xFFFFFFFFu, ex, off));
+  }
+  if ((threadIdx.x & 31) == 0 && local) {
+    atomicAdd(bad, local);
+    atomicMin(example, ex);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -577,11 +596,12 @@ cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* v
   return cudaGetLastError();
 }
 
-cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, cudaStream_t s) {
+cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsigned* example,
+                              cudaStream_t s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_cdiv_check<<<sms * 8, 256, 0, s>>>(y, zr, bad);
+  k_cdiv_check<<<sms * 8, 256, 0, s>>>(y, zr, bad, example);
   return cudaGetLastError();
 }
 

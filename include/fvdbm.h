@@ -150,6 +150,14 @@ int fvdbm_get_nodes(void *handle, float *pdf, float *rho, float *vel);
  * (src/containers.py:205-213).  flux [F][9]. */
 int fvdbm_get_face_fluxes(void *handle, float *flux);
 
+/* Self-test of the division by a known divisor that the kernels use for the
+ * lattice constants C^2, 2C^4 and 2C^2: counts, over all 2^32 float32
+ * dividends, those whose quotient differs in value from IEEE x / divisor on
+ * this device, and reports the lowest such bit pattern (0xFFFFFFFF if none).
+ * No counterpart in the reference (it divides with XLA's division). */
+int fvdbm_const_div_check(int32_t device, float divisor, uint64_t *mismatches,
+                          uint32_t *first_mismatch);
+
 /* Block until the handle's stream is idle; returns the device status. */
 int fvdbm_sync(void *handle);
 
