@@ -300,12 +300,16 @@ def run_gb300(args):
     cells_all = sum_over_ranks(float(N), ws, local)
     value = cells_all * K / (total_ms_max / 1e3) / 1e6
 
-    # the cell kernel's algorithmic bytes per launch: pdf read + write,
-    # cell->face slots, face geometry, ghost-node pdf read
+    # the dominant kernel's algorithmic bytes per launch: pdf read + write,
+    # cell->face slots, face geometry, boundary-node pdf traffic.  The tile
+    # kernel does the whole step in one launch.
     F = info["n_faces"]
     K3 = int(np.asarray(c.face_indices).shape[1])
-    cell_bytes = 72.0 * N + 4.0 * K3 * N + 20.0 * F + (8.0 * F if args.flux == "lax_wendroff" else 0.0) \
-        + 36.0 * info["n_bc_nodes"]
+    if info["kernel"] == 3:
+        cell_bytes = info["bytes_per_step"]
+    else:
+        cell_bytes = 72.0 * N + 4.0 * K3 * N + 20.0 * F + \
+            (8.0 * F if args.flux == "lax_wendroff" else 0.0) + 36.0 * info["n_bc_nodes"]
     cell_avg_s = statistics.mean(cell_ms) / 1e3
     peak, peak_kind = measured_peaks()
     achieved = cell_bytes / cell_avg_s / 1e9
@@ -352,7 +356,7 @@ def run_gb300(args):
     if rank == 0:
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                      "l2": "flushed between timed steps (2x L2 write on the step's stream)",
-                     "kernel": "fused" if info["kernel"] == 2 else "staged",
+                     "kernel": {1: "staged", 2: "fused", 3: "tile"}[info["kernel"]],
                      "launches_per_step": info["launches_per_step"]})
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "MCUPS", "n_gpus": ws, "steps": K,
@@ -361,7 +365,7 @@ def run_gb300(args):
             "config": desc,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": profiled_traffic("cell_kernel"),
-                         "kernel": "k_fused" if info["kernel"] == 2 else "k_gather",
+                         "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile"}[info["kernel"]],
                          "bytes_per_launch": cell_bytes, "avg_launch_us": round(cell_avg_s * 1e6, 3),
                          "peak_kind": peak_kind,
                          "step_frac": round(step_achieved / peak, 4),

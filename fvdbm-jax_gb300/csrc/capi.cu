@@ -44,6 +44,8 @@ struct Handle {
   float* mac = nullptr;  // rho [Np], vel [2][Np], feq [9][Np]
   long long steps_done = 0;
   bool fused = false;
+  bool tile = false;
+  int* status = nullptr;
   std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   std::string err;
@@ -162,15 +164,28 @@ int enqueue_steps(Handle* h, int n) {
   for (int s = 0; s < n; ++s) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
-    CK(launch_nodes(h->dp, fin, h->stream));
-    if (h->fused) {
-      CK(launch_fused(h->dp, fin, fout, h->stream));
+    if (h->tile) {
+      CK(launch_tile(h->dp, fin, fout, h->stream));
     } else {
-      CK(launch_face_flux(h->dp, fin, h->flux, h->stream));
-      CK(launch_gather(h->dp, fin, h->flux, fout, h->stream));
+      CK(launch_nodes(h->dp, fin, h->stream));
+      if (h->fused) {
+        CK(launch_fused(h->dp, fin, fout, h->stream));
+      } else {
+        CK(launch_face_flux(h->dp, fin, h->flux, h->stream));
+        CK(launch_gather(h->dp, fin, h->flux, fout, h->stream));
+      }
     }
     h->cur ^= 1;
   }
+  return FVDBM_OK;
+}
+
+int check_status(Handle* h) {
+  int st = 0;
+  CK(cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st != 0)
+    return fail(h, FVDBM_EDEVICE, "device status " + std::to_string(st) +
+                                      ": a bounded wait in the tile kernel gave up");
   return FVDBM_OK;
 }
 
@@ -261,11 +276,20 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   const HostPlan& hp = h->hp;
   DevPlan& p = h->dp;
   h->fused = hp.fusable && params->kernel != FVDBM_KERNEL_STAGED;
-  if (params->kernel == FVDBM_KERNEL_FUSED && !hp.fusable) {
-    h->err = "the fused kernel needs every cell face slot to name a face of that cell "
+  if ((params->kernel == FVDBM_KERNEL_FUSED || params->kernel == FVDBM_KERNEL_TILE) && !hp.fusable) {
+    h->err = "the fused kernels need every cell face slot to name a face of that cell "
              "and no per-q flux scale";
     return create_fail(h, FVDBM_EINVAL);
   }
+  const bool tile_possible = hp.fusable && hp.tile_ok && hp.K == 3;
+  if (params->kernel == FVDBM_KERNEL_TILE && !tile_possible) {
+    h->err = "the tile kernel needs triangles (3 face slots per cell) and at most " +
+             std::to_string(TILE_MAX_NODES) + " boundary nodes / " + std::to_string(TILE_MAX_ENTRIES) +
+             " node-stencil cells per tile of " + std::to_string(TILE) + " cells";
+    return create_fail(h, FVDBM_EINVAL);
+  }
+  h->tile = tile_possible &&
+            (params->kernel == FVDBM_KERNEL_TILE || params->kernel == FVDBM_KERNEL_AUTO);
   p.N = hp.N;
   p.Np = hp.Np;
   p.F = hp.F;
@@ -330,6 +354,25 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   UP(nd_w, hp.nd_w);
   UP(nd_sumw, hp.nd_sumw);
   UP(inv_area, hp.inv_area);
+  p.NT = hp.NT;
+  if (h->tile) {
+    UP(tn_ptr, hp.tn_ptr);
+    UP(tn_dev, hp.tn_dev);
+    UP(tn_kind, hp.tn_kind);
+    UP(tn_npad, hp.tn_npad);
+    UP(tn_e0, hp.tn_e0);
+    UP(tn_ecnt, hp.tn_ecnt);
+    UP(tn_sumw, hp.tn_sumw);
+    UP(te_ptr, hp.te_ptr);
+    UP(te_cell, hp.te_cell);
+    UP(te_w, hp.te_w);
+    UP(tgh_a, hp.tgh_a);
+    UP(tgh_b, hp.tgh_b);
+  }
+  if ((rc = dalloc<int>(h, &h->status, 1)) != FVDBM_OK) return create_fail(h, rc);
+  CR(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+  p.status = h->status;
+  if (h->tile) CR(prepare_tile(p));
   {
     float* d = nullptr;
     if ((rc = dalloc<float>(h, &d, size_t(Q) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
@@ -442,9 +485,11 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
   if (phase == 1) {
-    CK(launch_nodes(h->dp, fin, h->stream));
+    if (!h->tile) CK(launch_nodes(h->dp, fin, h->stream));
   } else if (phase == 2) {
-    if (h->fused) {
+    if (h->tile) {
+      CK(launch_tile(h->dp, fin, fout, h->stream));
+    } else if (h->fused) {
       CK(launch_fused(h->dp, fin, fout, h->stream));
     } else {
       CK(launch_face_flux(h->dp, fin, h->flux, h->stream));
@@ -463,7 +508,7 @@ int fvdbm_sync(void* handle) {
   Handle* h = static_cast<Handle*>(handle);
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  return FVDBM_OK;
+  return check_status(h);
 }
 
 int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf_eq) {
@@ -513,7 +558,8 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
       }
     }
   }
-  return FVDBM_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  return check_status(h);
 }
 
 int fvdbm_get_nodes(void* handle, float* pdf, float* rho, float* vel) {
@@ -573,8 +619,8 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED;
-  info->launches_per_step = (hp.Mc > 0 ? 1 : 0) + (h->fused ? 1 : 2);
+  info->kernel = h->tile ? FVDBM_KERNEL_TILE : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
+  info->launches_per_step = h->tile ? 1 : (hp.Mc > 0 ? 1 : 0) + (h->fused ? 1 : 2);
   info->padded_cells = hp.Np;
   info->const_division = (h->dp.d_c2.ok && h->dp.d_c4x2.ok && h->dp.d_c2x2.ok) ? 1 : 0;
   info->bytes_per_step = hp.bytes_per_step;

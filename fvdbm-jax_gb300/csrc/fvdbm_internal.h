@@ -22,6 +22,13 @@ constexpr int HF_GHOST = 1 << 3;
 constexpr int HF_SHIFT = 4;
 constexpr int64_t HF_MAX_INDEX = (int64_t(1) << 27) - 1;
 
+// Persistent tile kernel: TILE consecutive cells per CTA iteration; the
+// boundary nodes a tile's ghost faces need are evaluated inside the tile.
+constexpr int TILE = 256;
+constexpr int TILE_MAX_NODES = 128;    // nodes evaluated per tile
+constexpr int TILE_MAX_ENTRIES = 256;  // node-stencil cells per tile
+constexpr int TN_OWNER = 1 << 4;       // tn_kind flag: this tile writes the node state
+
 // Node-cell entry: cell index (device numbering); bit 31 marks an entry whose
 // reference index was -1 (its rho/vel gather wraps to the last cell but its
 // non-equilibrium part is zero, src/containers.py:388-390).
@@ -71,6 +78,16 @@ struct HostPlan {
   std::vector<float> nd_w, nd_sumw;
 
   std::vector<float> inv_area;  // [Np] when fv
+
+  // tile tables (valid when tile_ok)
+  bool tile_ok = false;
+  int NT = 0;
+  std::vector<int32_t> tn_ptr, tn_dev, tn_kind, tn_npad, tn_e0, tn_ecnt;
+  std::vector<float> tn_sumw;
+  std::vector<int32_t> te_ptr;
+  std::vector<uint32_t> te_cell;
+  std::vector<float> te_w;
+  std::vector<int32_t> tgh_a, tgh_b;  // ghost end nodes as tile-local indices
 
   bool finite_n = true;
   double bytes_per_step = 0.0;
@@ -135,12 +152,34 @@ struct DevPlan {
   float* node_rho;  // [Mp]
   float* node_vel;  // [2][Mp]
   const float* inv_area;
+  // tile kernel
+  int NT;
+  const int* tn_ptr;
+  const int* tn_dev;
+  const int* tn_kind;
+  const int* tn_npad;
+  const int* tn_e0;
+  const int* tn_ecnt;
+  const float* tn_sumw;
+  const int* te_ptr;
+  const unsigned* te_cell;
+  const float* te_w;
+  const int* tgh_a;
+  const int* tgh_b;
+  int* status;  // device status word (0 ok); set when a bounded wait gives up
 };
+
+constexpr int STATUS_WAIT_TIMEOUT = 1;
 
 // kernel launchers (kernels.cu)
 cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s);
 cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
 cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);
+// Persistent tile kernel (tile.cu): one launch per step.  prepare_tile sets
+// the kernel's shared-memory attribute and grid size; call it outside any
+// stream capture before the first launch_tile.
+cudaError_t prepare_tile(const DevPlan& p);
+cudaError_t launch_tile(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
 cudaError_t launch_gather(const DevPlan& p, const float* fin, const float* flux, float* fout,
                           cudaStream_t s);
 cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,

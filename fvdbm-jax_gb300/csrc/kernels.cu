@@ -1,201 +1,12 @@
-// FVDBM step kernels for sm_103a (GB300).
-//
-// Every kernel restates the reference's float32 arithmetic (MADALERAU/
-// FVDBM-JAX src/dynamics.py, src/containers.py, utils/utils.py) so that the
-// results are bitwise equal to the CPU oracle:
-//   * sums are left folds in the reference's index order;
-//   * the library is compiled with --fmad=false, so no multiply-add is
-//     contracted; the only FMAs are the explicit ones of cdiv();
-//   * rewrites are value-identical: the 0*x terms of the integer-lattice dot
-//     products only matter for non-finite inputs, and such inputs take the
-//     literal (faithful) path; the +-symmetric lattice directions reuse one
-//     quotient (RN(-a/c) == -RN(a/c)).
+// FVDBM step kernels for sm_103a (GB300): boundary nodes, the fused cell
+// kernel, the staged face/gather pair, read-back helpers and the division
+// self-check.  Arithmetic helpers live in fvdbm_math.cuh.
 //
 // Layout: cell pdfs are SoA [9][Np] float32 in device (renumbered) cell
 // order; node state is SoA [9][Mp]; per-cell face slots are SoA [K][Np].
-#include <cfloat>
-
-#include "fvdbm_internal.h"
+#include "fvdbm_math.cuh"
 
 namespace fvdbm {
-
-__constant__ float c_W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 9.0),
-                             (float)(1.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 36.0),
-                             (float)(1.0 / 36.0), (float)(1.0 / 36.0), (float)(1.0 / 36.0)};
-
-__device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
-
-// Correctly rounded x/y for a divisor known in advance.  With zr = RN(1/y):
-// q0 = RN(x*zr) is within 1.5 ulp of x/y; one correction
-// q1 = RN(q0 + RN(x - q0*y)*zr) (remainder exact through an FMA) makes it
-// faithful; by Markstein's theorem (P. Markstein, "Computation of elementary
-// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
-// 1990) a second correction q2 = RN(q1 + (x - q1*y)*zr) is then the correctly
-// rounded quotient (Brisebarre, Muller and Raina, IEEE Trans. Computers 53(8),
-// 2004, show that the first correction alone fails for some divisors).
-// Whether this equals x/y for every float32 x is checked exhaustively on the
-// device (k_cdiv_check) before the kernels are allowed to use it.
-__device__ __forceinline__ float cdiv_fast(float x, float y, float zr) {
-  const float q0 = __fmul_rn(x, zr);
-  const float r0 = __fmaf_rn(-q0, y, x);
-  const float q1 = __fmaf_rn(r0, zr, q0);
-  const float r1 = __fmaf_rn(-q1, y, x);
-  return __fmaf_rn(r1, zr, q1);
-}
-
-// The remainders are exact only while they stay above the subnormal range,
-// so tiny dividends (|x| < 2^-100) and quotients outside the normal range
-// take x/y; x == 0 gives +-0 either way.
-__device__ __forceinline__ float cdiv(float x, const CDiv& d) {
-  if (d.ok) {
-    const float q = cdiv_fast(x, d.y, d.zr);
-    const float a = fabsf(q);
-    if ((fabsf(x) >= 0x1p-100f && a >= FLT_MIN && a <= FLT_MAX) || x == 0.0f) return q;
-  }
-  return x / d.y;
-}
-
-// ---------------------------------------------------------------------------
-// Literal forms (src/dynamics.py:35-47,70-74), used for non-finite inputs.
-__device__ __forceinline__ void macros_literal(const float f[Q], float& mx, float& my) {
-  mx = 0.0f * f[0];
-  mx = mx + f[1];
-  mx = mx + 0.0f * f[2];
-  mx = mx + (-f[3]);
-  mx = mx + 0.0f * f[4];
-  mx = mx + f[5];
-  mx = mx + (-f[6]);
-  mx = mx + (-f[7]);
-  mx = mx + f[8];
-  my = 0.0f * f[0];
-  my = my + 0.0f * f[1];
-  my = my + f[2];
-  my = my + 0.0f * f[3];
-  my = my + (-f[4]);
-  my = my + f[5];
-  my = my + f[6];
-  my = my + (-f[7]);
-  my = my + (-f[8]);
-}
-
-// xi_q . (x, y) folded over the two components, 0*x terms kept
-__device__ __forceinline__ void xi_dot_literal(float x, float y, float a[Q]) {
-  const float zx = 0.0f * x, zy = 0.0f * y;
-  a[0] = zx + zy;
-  a[1] = x + zy;
-  a[2] = zx + y;
-  a[3] = (-x) + zy;
-  a[4] = zx + (-y);
-  a[5] = x + y;
-  a[6] = (-x) + y;
-  a[7] = (-x) + (-y);
-  a[8] = x + (-y);
-}
-
-__device__ __forceinline__ void feq9_literal(float rho, float ux, float uy, const DevPlan& p,
-                                          float out[Q]) {
-  float a[Q];
-  xi_dot_literal(ux, uy, a);
-  const float uu = ux * ux + uy * uy;
-  const float t = uu / p.c2x2;
-  for (int q = 0; q < Q; ++q) {
-    float s = 1.0f + a[q] / p.c2;
-    s = s + (a[q] * a[q]) / p.c4x2;
-    s = s - t;
-    out[q] = (c_W[q] * rho) * s;
-  }
-}
-
-// rho = sum_q f_q; u = (KSI^T f)/rho.  For finite rho every f_q is finite and
-// the 0*f_q terms of the literal fold are +-0, which leave the sum unchanged.
-__device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, float& uy) {
-  float r = f[0] + f[1];
-  r = r + f[2];
-  r = r + f[3];
-  r = r + f[4];
-  r = r + f[5];
-  r = r + f[6];
-  r = r + f[7];
-  r = r + f[8];
-  float mx, my;
-  if (finite(r)) {
-    mx = ((((f[1] - f[3]) + f[5]) - f[6]) - f[7]) + f[8];
-    my = ((((f[2] - f[4]) + f[5]) + f[6]) - f[7]) - f[8];
-  } else {
-    macros_literal(f, mx, my);
-  }
-  rho = r;
-  ux = mx / r;
-  uy = my / r;
-}
-
-// feq_q = (W_q rho) * (((1 + a_q/C^2) + a_q^2/(2C^4)) - u.u/(2C^2)).
-// With finite u: a_3 = -a_1, a_4 = -a_2, a_7 = -a_5, a_8 = -a_6 exactly, and
-// a_0 = +-0 gives s_0 = 1 - u.u/(2C^2).
-__device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPlan& p, float out[Q]) {
-  if (!(finite(ux) && finite(uy))) {
-    feq9_literal(rho, ux, uy, p, out);
-    return;
-  }
-  const float uu = ux * ux + uy * uy;
-  const float t = cdiv(uu, p.d_c2x2);
-  const float a5 = ux + uy, a6 = uy - ux;
-  const float x1 = cdiv(ux, p.d_c2), y1 = cdiv(ux * ux, p.d_c4x2);
-  const float x2 = cdiv(uy, p.d_c2), y2 = cdiv(uy * uy, p.d_c4x2);
-  const float x5 = cdiv(a5, p.d_c2), y5 = cdiv(a5 * a5, p.d_c4x2);
-  const float x6 = cdiv(a6, p.d_c2), y6 = cdiv(a6 * a6, p.d_c4x2);
-  float s[Q];
-  s[0] = 1.0f - t;
-  s[1] = ((1.0f + x1) + y1) - t;
-  s[3] = ((1.0f - x1) + y1) - t;
-  s[2] = ((1.0f + x2) + y2) - t;
-  s[4] = ((1.0f - x2) + y2) - t;
-  s[5] = ((1.0f + x5) + y5) - t;
-  s[7] = ((1.0f - x5) + y5) - t;
-  s[6] = ((1.0f + x6) + y6) - t;
-  s[8] = ((1.0f - x6) + y6) - t;
-#pragma unroll
-  for (int q = 0; q < Q; ++q) out[q] = (c_W[q] * rho) * s[q];
-}
-
-// v_q = xi_q . n (src/containers.py:235); symmetric form for finite n
-__device__ __forceinline__ void xi_dot_n(float nx, float ny, bool finite_n, float v[Q]) {
-  if (!finite_n) {
-    xi_dot_literal(nx, ny, v);
-    return;
-  }
-  const float s = nx + ny, d = ny - nx;
-  v[0] = 0.0f;
-  v[1] = nx;
-  v[2] = ny;
-  v[3] = -nx;
-  v[4] = -ny;
-  v[5] = s;
-  v[6] = d;
-  v[7] = -s;
-  v[8] = -d;
-}
-
-// Lax-Wendroff weights interp_q = d0/(d0+d1) - (v_q*dt)/(2(d0+d1))
-// (src/containers.py:274); (-v*dt)/D2 == -((v*dt)/D2).
-__device__ __forceinline__ void lw_interp(const float v[Q], float r, float D2, float dt,
-                                          bool finite_n, float w[Q]) {
-  if (!finite_n) {
-    for (int q = 0; q < Q; ++q) w[q] = r - (v[q] * dt) / D2;
-    return;
-  }
-  const float t1 = (v[1] * dt) / D2, t2 = (v[2] * dt) / D2;
-  const float t5 = (v[5] * dt) / D2, t6 = (v[6] * dt) / D2;
-  w[0] = r - (v[0] * dt) / D2;
-  w[1] = r - t1;
-  w[3] = r + t1;
-  w[2] = r - t2;
-  w[4] = r + t2;
-  w[5] = r - t5;
-  w[7] = r + t5;
-  w[6] = r - t6;
-  w[8] = r + t6;
-}
 
 // ---------------------------------------------------------------------------
 // Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  One group of

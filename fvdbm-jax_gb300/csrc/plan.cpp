@@ -154,7 +154,7 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
   hp.P = P;
   hp.K = K;
   hp.Kn = Kn;
-  hp.Np = std::max(128, round_up(N, 128));
+  hp.Np = std::max(TILE, round_up(N, TILE));
   hp.Fp = std::max(128, round_up(F, 128));
   hp.scheme = pr.flux_scheme;
   hp.variant = pr.variant;
@@ -399,6 +399,84 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       if (pr.variant == 1) hp.hf_scale[s] = hp.fscale[j];
     }
   }
+  // ---- tile tables: per tile the nodes its ghost faces need (plus owner-only
+  // computed nodes that no ghost face uses), their stencil entries, and the
+  // ghost end nodes as tile-local indices
+  if (hp.fusable && N > 0) {
+    const int NT = (N + TILE - 1) / TILE;
+    const int G = int(hp.gh_a.size());
+    std::vector<char> referenced(hp.M, 0);
+    for (int g = 0; g < G; ++g) referenced[hp.gh_a[g]] = referenced[hp.gh_b[g]] = 1;
+    std::vector<std::vector<int32_t>> extra(NT);
+    for (int d = 0; d < hp.Mc; ++d)
+      if (!referenced[d]) {
+        int t = 0;
+        if (hp.nd_ptr[d + 1] > hp.nd_ptr[d]) t = int(hp.nd_cell[hp.nd_ptr[d]] & ~ND_NEQ_ZERO) / TILE;
+        extra[t].push_back(d);
+      }
+    std::vector<int32_t> mark(hp.M, -1), local(hp.M, -1);
+    std::vector<char> owned(hp.M, 0);
+    hp.tgh_a.assign(G, 0);
+    hp.tgh_b.assign(G, 0);
+    hp.tn_ptr.assign(1, 0);
+    hp.te_ptr.assign(1, 0);
+    bool ok = true;
+    for (int t = 0; t < NT && ok; ++t) {
+      std::vector<int32_t> list;
+      auto add = [&](int32_t d) {
+        if (mark[d] != t) {
+          mark[d] = t;
+          local[d] = int(list.size());
+          list.push_back(d);
+        }
+      };
+      const int i1 = std::min(N, (t + 1) * TILE);
+      for (int i = t * TILE; i < i1; ++i)
+        for (int k = 0; k < K; ++k) {
+          const int32_t code = hp.hf_code[size_t(k) * hp.Np + i];
+          if (!(code & HF_GHOST)) continue;
+          const int g = code >> HF_SHIFT;
+          add(hp.gh_a[g]);
+          add(hp.gh_b[g]);
+          hp.tgh_a[g] = local[hp.gh_a[g]];
+          hp.tgh_b[g] = local[hp.gh_b[g]];
+        }
+      for (int32_t d : extra[t]) add(d);
+      const int e_start = int(hp.te_cell.size());
+      for (int32_t d : list) {
+        int kind = 0, npad = 0, e0 = 0, ecnt = 0;
+        float sumw = 0.0f;
+        if (d < hp.Mc) {
+          kind = hp.nd_type[d];
+          if (!owned[d]) {
+            owned[d] = 1;
+            kind |= TN_OWNER;
+          }
+          sumw = hp.nd_sumw[d];
+          npad = hp.nd_npad[d];
+          e0 = int(hp.te_cell.size()) - e_start;
+          for (int j = hp.nd_ptr[d]; j < hp.nd_ptr[d + 1]; ++j) {
+            hp.te_cell.push_back(hp.nd_cell[j]);
+            hp.te_w.push_back(hp.nd_w[j]);
+          }
+          ecnt = hp.nd_ptr[d + 1] - hp.nd_ptr[d];
+        }
+        hp.tn_dev.push_back(d);
+        hp.tn_kind.push_back(kind);
+        hp.tn_npad.push_back(npad);
+        hp.tn_e0.push_back(e0);
+        hp.tn_ecnt.push_back(ecnt);
+        hp.tn_sumw.push_back(sumw);
+      }
+      if (int(list.size()) > TILE_MAX_NODES || int(hp.te_cell.size()) - e_start > TILE_MAX_ENTRIES)
+        ok = false;
+      hp.tn_ptr.push_back(int(hp.tn_dev.size()));
+      hp.te_ptr.push_back(int(hp.te_cell.size()));
+    }
+    hp.NT = NT;
+    hp.tile_ok = ok;
+  }
+
   if (hp.fv) {
     hp.inv_area.assign(hp.Np, 0.0f);
     for (int i = 0; i < N; ++i) hp.inv_area[i] = m.cell_inv_area[hp.cell_old[i]];

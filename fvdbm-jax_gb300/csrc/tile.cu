@@ -1,0 +1,403 @@
+// Persistent tile kernel: one launch per FVDBM step (sm_103a).
+//
+// The cells are cut into tiles of TILE consecutive cells (device order, which
+// is Morton order when centroids are known).  Each CTA walks its tiles; for
+// each tile one thread issues bulk async copies (cp.async.bulk, completion
+// counted on an mbarrier) of the tile's 9 pdf rows and its per-face-slot rows
+// (neighbour code, normal, signed length, and the Lax-Wendroff / stencil
+// scale rows when used) into shared memory, double-buffered so that the next
+// tile streams in while this one computes.  Then:
+//   phase A  the boundary nodes that the tile's ghost faces need
+//            (Nodes.calc_pdfs, src/containers.py:339-404): one thread per
+//            node-stencil entry evaluates that cell's macros, equilibrium and
+//            IDW products into shared memory; one thread per node folds them
+//            in the reference's entry order.  The tile that owns a node also
+//            writes its state to global memory for read-back;
+//   phase B  one thread per cell: macros, equilibrium, the three face fluxes
+//            (neighbour pdfs from shared memory when inside the tile) and the
+//            update (src/containers.py:107-121, :191-291).
+// Arithmetic is that of fvdbm_math.cuh, so the result is bitwise equal to the
+// CPU oracle and to the two-kernel path.
+//
+// Every mbarrier wait is bounded; a wait that gives up sets p.status, waits
+// (bounded) for the CTA's copies still in flight and returns.
+#include "fvdbm_math.cuh"
+
+namespace fvdbm {
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity), "r"(1000u)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait: ~1000 ns suspend hint per try, 2^21 tries.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 21); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+template <int SCHEME, int VARIANT>
+struct TileRows {
+  static constexpr int K = 3;
+  static constexpr int F = 0;               // 9 pdf rows
+  static constexpr int CODE = 9;            // K rows each
+  static constexpr int NX = CODE + K;
+  static constexpr int NY = NX + K;
+  static constexpr int LS = NY + K;
+  static constexpr int R = LS + K;          // Lax-Wendroff d0/(d0+d1)
+  static constexpr int D2 = R + (SCHEME == 1 ? K : 0);
+  static constexpr int SC = D2 + (SCHEME == 1 ? K : 0);
+  static constexpr int ROWS = SC + (VARIANT == 1 ? K : 0);
+};
+
+template <int SCHEME, int VARIANT>
+__device__ __forceinline__ const void* row_src(const DevPlan& p, const float* fin, int r) {
+  using RW = TileRows<SCHEME, VARIANT>;
+  const size_t Np = p.Np;
+  if (r < RW::CODE) return fin + size_t(r) * Np;
+  if (r < RW::NX) return p.hf_code + size_t(r - RW::CODE) * Np;
+  if (r < RW::NY) return p.hf_nx + size_t(r - RW::NX) * Np;
+  if (r < RW::LS) return p.hf_ny + size_t(r - RW::NY) * Np;
+  if (r < RW::R) return p.hf_L + size_t(r - RW::LS) * Np;
+  if (SCHEME == 1 && r < RW::D2) return p.hf_r + size_t(r - RW::R) * Np;
+  if (SCHEME == 1 && r < RW::SC) return p.hf_D2 + size_t(r - RW::D2) * Np;
+  return p.hf_scale + size_t(r - RW::SC) * Np;
+}
+
+template <int SCHEME, int VARIANT>
+__device__ __forceinline__ void issue_tile(const DevPlan& p, const float* fin, int tile, float* stage,
+                                           uint32_t bar) {
+  using RW = TileRows<SCHEME, VARIANT>;
+  constexpr uint32_t row_bytes = TILE * sizeof(float);
+  mbar_expect_tx(bar, RW::ROWS * row_bytes);
+  const size_t off = size_t(tile) * TILE;
+#pragma unroll 1
+  for (int r = 0; r < RW::ROWS; ++r) {
+    const float* src = static_cast<const float*>(row_src<SCHEME, VARIANT>(p, fin, r)) + off;
+    bulk_g2s(smem_u32(stage + r * TILE), src, row_bytes, bar);
+  }
+}
+
+}  // namespace
+
+template <int SCHEME, int VARIANT>
+constexpr size_t tile_smem_bytes() {
+  return (size_t(2) * TileRows<SCHEME, VARIANT>::ROWS * TILE + size_t(Q) * TILE_MAX_NODES +
+          size_t(12) * TILE_MAX_ENTRIES) * sizeof(float) + 2 * sizeof(uint64_t);
+}
+
+template <int SCHEME, int VARIANT, bool FV>
+__global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __restrict__ fin,
+                                                  float* __restrict__ fout) {
+  using RW = TileRows<SCHEME, VARIANT>;
+  constexpr int K = RW::K;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* stage0 = reinterpret_cast<float*>(smem_raw);
+  float* npdf = stage0 + 2 * RW::ROWS * TILE;      // [9][TILE_MAX_NODES]
+  float* prod = npdf + Q * TILE_MAX_NODES;          // [12][TILE_MAX_ENTRIES]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(prod + 12 * TILE_MAX_ENTRIES);
+  const int tid = threadIdx.x;
+  const int first = blockIdx.x, stride = gridDim.x;
+  if (first >= p.NT) return;
+  const size_t Np = p.Np;
+  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+
+  if (tid == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    issue_tile<SCHEME, VARIANT>(p, fin, first, stage0, bar0);
+    if (first + stride < p.NT)
+      issue_tile<SCHEME, VARIANT>(p, fin, first + stride, stage0 + RW::ROWS * TILE, bar1);
+  }
+
+  int it = 0;
+  for (int t = first; t < p.NT; t += stride, ++it) {
+    const int s = it & 1;
+    const uint32_t bar = s ? bar1 : bar0;
+    const uint32_t parity = (it >> 1) & 1;
+    const bool timed_out = !mbar_wait(bar, parity);
+    if (__syncthreads_or(timed_out)) {
+      // give up: report, let the copies still in flight land, return
+      if (tid == 0) {
+        atomicExch(p.status, STATUS_WAIT_TIMEOUT);
+        if (t + stride < p.NT) mbar_wait(s ? bar0 : bar1, ((it + 1) >> 1) & 1);
+        mbar_wait(bar, parity);
+      }
+      __syncthreads();
+      return;
+    }
+    const float* S = stage0 + s * RW::ROWS * TILE;
+    const int tile_start = t * TILE;
+
+    // ---- phase A: boundary nodes needed by this tile
+    const int nb = __ldg(p.tn_ptr + t), nn = __ldg(p.tn_ptr + t + 1) - nb;
+    if (nn > 0) {
+      const int eb = __ldg(p.te_ptr + t), ne = __ldg(p.te_ptr + t + 1) - eb;
+      if (tid < ne) {
+        const unsigned code = __ldg(p.te_cell + eb + tid);
+        const int c = int(code & ~ND_NEQ_ZERO);
+        const float w = __ldg(p.te_w + eb + tid);
+        float fc[Q], eq[Q];
+        const unsigned lc = unsigned(c - tile_start);
+        if (lc < unsigned(TILE)) {
+#pragma unroll
+          for (int q = 0; q < Q; ++q) fc[q] = S[(RW::F + q) * TILE + lc];
+        } else {
+#pragma unroll
+          for (int q = 0; q < Q; ++q) fc[q] = __ldg(fin + q * Np + c);
+        }
+        float rho, ux, uy;
+        macros(fc, rho, ux, uy);
+        feq9(rho, ux, uy, p, eq);
+        const bool zero = (code & ND_NEQ_ZERO) != 0;
+        prod[0 * TILE_MAX_ENTRIES + tid] = rho * w;
+        prod[1 * TILE_MAX_ENTRIES + tid] = ux * w;
+        prod[2 * TILE_MAX_ENTRIES + tid] = uy * w;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+          prod[(3 + q) * TILE_MAX_ENTRIES + tid] = (zero ? 0.0f : fc[q] - eq[q]) * w;
+      }
+      __syncthreads();
+      if (tid < nn) {
+        const int kind = __ldg(p.tn_kind + nb + tid);
+        const int d = __ldg(p.tn_dev + nb + tid);
+        const int type = kind & 3;
+        float g[Q];
+        if (type == 0) {
+#pragma unroll
+          for (int q = 0; q < Q; ++q) g[q] = p.node_pdf[size_t(q) * p.Mp + d];
+        } else {
+          const int e0 = __ldg(p.tn_e0 + nb + tid), cnt = __ldg(p.tn_ecnt + nb + tid);
+          float ar = 0.0f, ax = 0.0f, ay = 0.0f, an[Q];
+#pragma unroll
+          for (int q = 0; q < Q; ++q) an[q] = 0.0f;
+          for (int j = 0; j < cnt; ++j) {
+            const int e = e0 + j;
+            const float vr = prod[0 * TILE_MAX_ENTRIES + e];
+            const float vx = prod[1 * TILE_MAX_ENTRIES + e];
+            const float vy = prod[2 * TILE_MAX_ENTRIES + e];
+            ar = j ? ar + vr : vr;
+            ax = j ? ax + vx : vx;
+            ay = j ? ay + vy : vy;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+              const float vn = prod[(3 + q) * TILE_MAX_ENTRIES + e];
+              an[q] = j ? an[q] + vn : vn;
+            }
+          }
+          if (__ldg(p.tn_npad + nb + tid) > 0) {
+            // padded (-1, weight 0) entries gather the last cell: rho*0, u*0
+            float fc[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) fc[q] = __ldg(fin + q * Np + p.last_cell);
+            float rho, ux, uy;
+            macros(fc, rho, ux, uy);
+            ar = cnt ? ar + rho * 0.0f : rho * 0.0f;
+            ax = cnt ? ax + ux * 0.0f : ux * 0.0f;
+            ay = cnt ? ay + uy * 0.0f : uy * 0.0f;
+          }
+          const float sw = __ldg(p.tn_sumw + nb + tid);
+          float rho_p, ux_p, uy_p;
+          if (type == 1) {
+            rho_p = ar / sw;
+            ux_p = p.node_vel[d];
+            uy_p = p.node_vel[p.Mp + d];
+          } else {
+            rho_p = p.node_rho[d];
+            ux_p = ax / sw;
+            uy_p = ay / sw;
+          }
+          float eqn[Q];
+          feq9(rho_p, ux_p, uy_p, p, eqn);
+#pragma unroll
+          for (int q = 0; q < Q; ++q) g[q] = eqn[q] + an[q] / sw;
+          if (kind & TN_OWNER) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) p.node_pdf[size_t(q) * p.Mp + d] = g[q];
+            if (type == 1) {
+              p.node_rho[d] = rho_p;
+            } else {
+              p.node_vel[d] = ux_p;
+              p.node_vel[p.Mp + d] = uy_p;
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) npdf[q * TILE_MAX_NODES + tid] = g[q];
+      }
+      __syncthreads();
+    }
+
+    // ---- phase B: the tile's cells
+    const int i = tile_start + tid;
+    if (i < p.N) {
+      float f[Q];
+#pragma unroll
+      for (int q = 0; q < Q; ++q) f[q] = S[(RW::F + q) * TILE + tid];
+      float rho, ux, uy, eq[Q];
+      macros(f, rho, ux, uy);
+      feq9(rho, ux, uy, p, eq);
+      float acc[Q];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int code = __float_as_int(S[(RW::CODE + k) * TILE + tid]);
+        const float nx = S[(RW::NX + k) * TILE + tid];
+        const float ny = S[(RW::NY + k) * TILE + tid];
+        const float Ls = S[(RW::LS + k) * TILE + tid];
+        const int other = code >> HF_SHIFT;
+        const bool slot1 = (code & HF_SLOT1) != 0;
+        float o[Q];
+        if (code & HF_GHOST) {
+          const int la = __ldg(p.tgh_a + other), lb = __ldg(p.tgh_b + other);
+          const float rg = __ldg(p.gh_r + other);
+#pragma unroll
+          for (int q = 0; q < Q; ++q) {
+            const float mq = (npdf[q * TILE_MAX_NODES + la] + npdf[q * TILE_MAX_NODES + lb]) / 2.0f;
+            o[q] = mq + (mq - f[q]) * rg;
+          }
+        } else {
+          const unsigned lo = unsigned(other - tile_start);
+          if (lo < unsigned(TILE)) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) o[q] = S[(RW::F + q) * TILE + lo];
+          } else {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) o[q] = __ldg(fin + q * Np + other);
+          }
+        }
+        float v[Q], w[Q];
+        xi_dot_n(nx, ny, p.finite_n != 0, v);
+        if (SCHEME == 1)
+          lw_interp(v, S[(RW::R + k) * TILE + tid], S[(RW::D2 + k) * TILE + tid], p.dt,
+                    p.finite_n != 0, w);
+        const float scale = (VARIANT == 1) ? S[(RW::SC + k) * TILE + tid] : 1.0f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          float phi;
+          if (SCHEME == 0) {
+            phi = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
+          } else {
+            const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
+            phi = lq + (rq - lq) * w[q];
+          }
+          float x = (phi * v[q]) * Ls;
+          if (VARIANT == 1) x = x * scale;
+          acc[q] = (k == 0) ? x : acc[q] + x;
+        }
+      }
+      if (FV) {
+        const float ia = __ldg(p.inv_area + i);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
+      }
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+        fout[q * Np + i] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+    }
+
+    // ---- refill this stage with the tile two steps ahead
+    __syncthreads();
+    const int tn = t + 2 * stride;
+    if (tid == 0 && tn < p.NT) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue_tile<SCHEME, VARIANT>(p, fin, tn, stage0 + s * RW::ROWS * TILE, bar);
+    }
+  }
+}
+
+namespace {
+
+// Grid = SMs x resident CTAs per SM, per instantiation and device.
+template <int S, int V, bool FV>
+struct TileLaunch {
+  static int grid[64];
+
+  static cudaError_t prepare() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (grid[dev] > 0) return cudaSuccess;
+    constexpr size_t smem = tile_smem_bytes<S, V>();
+    e = cudaFuncSetAttribute(k_tile<S, V, FV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    int sms = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<S, V, FV>, TILE, smem);
+    if (e != cudaSuccess) return e;
+    grid[dev] = sms * (per_sm > 0 ? per_sm : 1);
+    return cudaSuccess;
+  }
+
+  static cudaError_t launch(const DevPlan& p, const float* fin, float* fout, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || grid[dev] <= 0) return cudaErrorNotReady;
+    const int g = grid[dev] < p.NT ? grid[dev] : p.NT;
+    k_tile<S, V, FV><<<g, TILE, tile_smem_bytes<S, V>(), st>>>(p, fin, fout);
+    return cudaGetLastError();
+  }
+};
+
+template <int S, int V, bool FV>
+int TileLaunch<S, V, FV>::grid[64] = {0};
+
+template <class Fn>
+cudaError_t dispatch(const DevPlan& p, Fn&& fn) {
+  if (p.scheme == 0 && p.variant == 0) return p.fv ? fn(TileLaunch<0, 0, true>{}) : fn(TileLaunch<0, 0, false>{});
+  if (p.scheme == 1 && p.variant == 0) return p.fv ? fn(TileLaunch<1, 0, true>{}) : fn(TileLaunch<1, 0, false>{});
+  if (p.scheme == 0 && p.variant == 1) return p.fv ? fn(TileLaunch<0, 1, true>{}) : fn(TileLaunch<0, 1, false>{});
+  if (p.scheme == 1 && p.variant == 1) return p.fv ? fn(TileLaunch<1, 1, true>{}) : fn(TileLaunch<1, 1, false>{});
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t prepare_tile(const DevPlan& p) {
+  if (p.K != 3) return cudaErrorInvalidValue;
+  return dispatch(p, [](auto L) { return decltype(L)::prepare(); });
+}
+
+cudaError_t launch_tile(const DevPlan& p, const float* fin, float* fout, cudaStream_t st) {
+  if (p.N == 0 || p.NT == 0) return cudaSuccess;
+  if (p.K != 3) return cudaErrorInvalidValue;
+  return dispatch(p, [&](auto L) { return decltype(L)::launch(p, fin, fout, st); });
+}
+
+}  // namespace fvdbm

@@ -32,7 +32,8 @@ from .dynamics import D2Q9
 F32, I32 = np.float32, np.int32
 
 _ORDER = {"none": nat.ORDER_NONE, "rcm": nat.ORDER_RCM, "morton": nat.ORDER_MORTON}
-_KERNEL = {"auto": nat.KERNEL_AUTO, "staged": nat.KERNEL_STAGED, "fused": nat.KERNEL_FUSED}
+_KERNEL = {"auto": nat.KERNEL_AUTO, "staged": nat.KERNEL_STAGED, "fused": nat.KERNEL_FUSED,
+           "tile": nat.KERNEL_TILE}
 
 
 def _face_scale(faces):

@@ -58,9 +58,10 @@ extern "C" {
 #define FVDBM_ORDER_MORTON 2 /* Z-order of cell_xy (needs cell_xy) */
 
 /* Kernel family for the step. */
-#define FVDBM_KERNEL_AUTO 0   /* fused when the mesh allows it, else staged */
+#define FVDBM_KERNEL_AUTO 0   /* tile when the mesh allows it, else fused, else staged */
 #define FVDBM_KERNEL_STAGED 1 /* node BC + face flux + cell gather (3 kernels) */
 #define FVDBM_KERNEL_FUSED 2  /* node BC + fused cell kernel (2 kernels) */
+#define FVDBM_KERNEL_TILE 3   /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {
@@ -158,7 +159,9 @@ int fvdbm_get_face_fluxes(void *handle, float *flux);
 int fvdbm_const_div_check(int32_t device, float divisor, uint64_t *mismatches,
                           uint32_t *first_mismatch);
 
-/* Block until the handle's stream is idle; returns the device status. */
+/* Block until the handle's stream is idle.  Returns FVDBM_EDEVICE when a
+ * kernel reported a failure on the device status word (a bounded wait that
+ * gave up), else 0 or a CUDA error. */
 int fvdbm_sync(void *handle);
 
 /* The handle's cudaStream_t (for event timing by the caller). */

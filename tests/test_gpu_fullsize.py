@@ -68,7 +68,7 @@ def test_channel_config_bitwise(flux):
     from fvdbm_jax_gb300 import Environment, meshgen
     m, dyn, c, f, n = _case(meshgen.channel_cylinder(), flux, tau=0.55, bc="channel")
     ref = _oracle(c, f, n, dyn, 100)
-    for kernel in ("fused", "staged"):
+    for kernel in ("tile", "fused", "staged"):
         env = Environment(c, f, n, kernel=kernel)
         env.init()
         env.step(100)
@@ -83,6 +83,7 @@ def test_porous_1m_bitwise_and_deterministic():
     ref = _oracle(c, f, n, dyn, 4)
     env = Environment(c, f, n)
     env.init()
+    assert env.info()["kernel"] == 3  # the tile kernel, several tiles per CTA
     env.step(4)
     _compare(env, ref)
     a = np.array(env.cells.pdf)
@@ -90,6 +91,10 @@ def test_porous_1m_bitwise_and_deterministic():
     env2.init()
     env2.step(4)
     assert np.array_equal(np.array(env2.cells.pdf), a)
+    env3 = Environment(c, f, n, kernel="fused")
+    env3.init()
+    env3.step(4)
+    assert np.array_equal(np.array(env3.cells.pdf), a)
 
 
 def test_graph_and_eager_steps_agree():
