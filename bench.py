@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "staged", "tile", "tile_split"])
     return ap.parse_args()
 
 
@@ -257,7 +258,7 @@ def run_gb300(args):
     ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
     m, dyn, c, f, n, desc = workload(args.workload, args.flux, seed=rank)
-    env = Environment(c, f, n, device=local)
+    env = Environment(c, f, n, device=local, kernel=args.kernel)
     env.init()
     info = env.info()
     L = nat.lib()
@@ -307,6 +308,8 @@ def run_gb300(args):
     K3 = int(np.asarray(c.face_indices).shape[1])
     if info["kernel"] == 3:
         cell_bytes = info["bytes_per_step"]
+    elif info["kernel"] == 4:
+        cell_bytes = info["bytes_per_step"] - 36.0 * info["n_bc_nodes"]
     else:
         cell_bytes = 72.0 * N + 4.0 * K3 * N + 20.0 * F + \
             (8.0 * F if args.flux == "lax_wendroff" else 0.0) + 36.0 * info["n_bc_nodes"]
@@ -356,8 +359,9 @@ def run_gb300(args):
     if rank == 0:
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                      "l2": "flushed between timed steps (2x L2 write on the step's stream)",
-                     "kernel": {1: "staged", 2: "fused", 3: "tile"}[info["kernel"]],
-                     "launches_per_step": info["launches_per_step"]})
+                     "kernel": {1: "staged", 2: "fused", 3: "tile", 4: "tile_split"}[info["kernel"]],
+                     "launches_per_step": info["launches_per_step"],
+                     "ctas_per_sm": info["ctas_per_sm"]})
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "MCUPS", "n_gpus": ws, "steps": K,
             "warmup": args.warmup, "ms_per_step": round(total_ms_max / K, 5), "higher_is_better": True,
@@ -365,7 +369,7 @@ def run_gb300(args):
             "config": desc,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": profiled_traffic("cell_kernel"),
-                         "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile"}[info["kernel"]],
+                         "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile", 4: "k_tile"}[info["kernel"]],
                          "bytes_per_launch": cell_bytes, "avg_launch_us": round(cell_avg_s * 1e6, 3),
                          "peak_kind": peak_kind,
                          "step_frac": round(step_achieved / peak, 4),

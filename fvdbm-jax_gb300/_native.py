@@ -16,7 +16,7 @@ from . import build as _build
 FVDBM_UPWIND, FVDBM_LAX_WENDROFF = 0, 1
 VARIANT_NONE, VARIANT_FACE_SCALE, VARIANT_FACE_Q_SCALE = 0, 1, 2
 ORDER_NONE, ORDER_RCM, ORDER_MORTON = 0, 1, 2
-KERNEL_AUTO, KERNEL_STAGED, KERNEL_FUSED, KERNEL_TILE = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_STAGED, KERNEL_FUSED, KERNEL_TILE, KERNEL_TILE_SPLIT = 0, 1, 2, 3, 4
 
 _i32p = C.POINTER(C.c_int32)
 _f32p = C.POINTER(C.c_float)
@@ -47,7 +47,8 @@ class Info(C.Structure):
     _fields_ = [
         ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_nodes", C.c_int32),
         ("n_bc_nodes", C.c_int32), ("n_ghost_faces", C.c_int32), ("kernel", C.c_int32),
-        ("launches_per_step", C.c_int32), ("padded_cells", C.c_int32), ("const_division", C.c_int32),
+        ("launches_per_step", C.c_int32), ("padded_cells", C.c_int32), ("ctas_per_sm", C.c_int32),
+        ("const_division", C.c_int32),
         ("bytes_per_step", C.c_double), ("device_bytes", C.c_double),
     ]
 

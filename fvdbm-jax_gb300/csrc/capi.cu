@@ -165,6 +165,7 @@ int enqueue_steps(Handle* h, int n) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
     if (h->tile) {
+      if (!h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
       CK(launch_tile(h->dp, fin, fout, h->stream));
     } else {
       CK(launch_nodes(h->dp, fin, h->stream));
@@ -276,20 +277,22 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   const HostPlan& hp = h->hp;
   DevPlan& p = h->dp;
   h->fused = hp.fusable && params->kernel != FVDBM_KERNEL_STAGED;
-  if ((params->kernel == FVDBM_KERNEL_FUSED || params->kernel == FVDBM_KERNEL_TILE) && !hp.fusable) {
+  const bool want_tile = params->kernel == FVDBM_KERNEL_TILE || params->kernel == FVDBM_KERNEL_TILE_SPLIT;
+  if ((params->kernel == FVDBM_KERNEL_FUSED || want_tile) && !hp.fusable) {
     h->err = "the fused kernels need every cell face slot to name a face of that cell "
              "and no per-q flux scale";
     return create_fail(h, FVDBM_EINVAL);
   }
-  const bool tile_possible = hp.fusable && hp.tile_ok && hp.K == 3;
-  if (params->kernel == FVDBM_KERNEL_TILE && !tile_possible) {
+  const bool tile_possible = hp.fusable && hp.K == 3 && hp.N > 0 &&
+                             (params->kernel != FVDBM_KERNEL_TILE || hp.tile_ok);
+  if (want_tile && !tile_possible) {
     h->err = "the tile kernel needs triangles (3 face slots per cell) and at most " +
              std::to_string(TILE_MAX_NODES) + " boundary nodes / " + std::to_string(TILE_MAX_ENTRIES) +
              " node-stencil cells per tile of " + std::to_string(TILE) + " cells";
     return create_fail(h, FVDBM_EINVAL);
   }
-  h->tile = tile_possible &&
-            (params->kernel == FVDBM_KERNEL_TILE || params->kernel == FVDBM_KERNEL_AUTO);
+  h->tile = tile_possible && want_tile;
+  h->dp.tile_nodes = (params->kernel == FVDBM_KERNEL_TILE) ? 1 : 0;
   p.N = hp.N;
   p.Np = hp.Np;
   p.F = hp.F;
@@ -485,7 +488,7 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
   if (phase == 1) {
-    if (!h->tile) CK(launch_nodes(h->dp, fin, h->stream));
+    if (!h->tile || !h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
   } else if (phase == 2) {
     if (h->tile) {
       CK(launch_tile(h->dp, fin, fout, h->stream));
@@ -619,9 +622,12 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->tile ? FVDBM_KERNEL_TILE : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
-  info->launches_per_step = h->tile ? 1 : (hp.Mc > 0 ? 1 : 0) + (h->fused ? 1 : 2);
+  info->kernel = h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
+                          : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
+  const int node_launch = (hp.Mc > 0 && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
+  info->launches_per_step = node_launch + (h->tile ? 1 : (h->fused ? 1 : 2));
   info->padded_cells = hp.Np;
+  info->ctas_per_sm = h->tile ? tile_ctas_per_sm(h->dp) : 0;
   info->const_division = (h->dp.d_c2.ok && h->dp.d_c4x2.ok && h->dp.d_c2x2.ok) ? 1 : 0;
   info->bytes_per_step = hp.bytes_per_step;
   info->device_bytes = h->device_bytes;

@@ -154,6 +154,7 @@ struct DevPlan {
   const float* inv_area;
   // tile kernel
   int NT;
+  int tile_nodes;  // boundary nodes evaluated inside the tile kernel (else by k_nodes)
   const int* tn_ptr;
   const int* tn_dev;
   const int* tn_kind;
@@ -179,6 +180,7 @@ cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cuda
 // the kernel's shared-memory attribute and grid size; call it outside any
 // stream capture before the first launch_tile.
 cudaError_t prepare_tile(const DevPlan& p);
+int tile_ctas_per_sm(const DevPlan& p);
 cudaError_t launch_tile(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
 cudaError_t launch_gather(const DevPlan& p, const float* fin, const float* flux, float* fout,
                           cudaStream_t s);

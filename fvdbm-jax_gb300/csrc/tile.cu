@@ -95,17 +95,20 @@ __device__ __forceinline__ const void* row_src(const DevPlan& p, const float* fi
   return p.hf_scale + size_t(r - RW::SC) * Np;
 }
 
+// Called by all 32 lanes of warp 0: lane 0 posts the byte count, then the
+// lanes issue one row copy each (ROWS <= 32).
 template <int SCHEME, int VARIANT>
 __device__ __forceinline__ void issue_tile(const DevPlan& p, const float* fin, int tile, float* stage,
-                                           uint32_t bar) {
+                                           uint32_t bar, int lane) {
   using RW = TileRows<SCHEME, VARIANT>;
+  static_assert(RW::ROWS <= 32, "one row per lane");
   constexpr uint32_t row_bytes = TILE * sizeof(float);
-  mbar_expect_tx(bar, RW::ROWS * row_bytes);
-  const size_t off = size_t(tile) * TILE;
-#pragma unroll 1
-  for (int r = 0; r < RW::ROWS; ++r) {
-    const float* src = static_cast<const float*>(row_src<SCHEME, VARIANT>(p, fin, r)) + off;
-    bulk_g2s(smem_u32(stage + r * TILE), src, row_bytes, bar);
+  if (lane == 0) mbar_expect_tx(bar, RW::ROWS * row_bytes);
+  __syncwarp();
+  if (lane < RW::ROWS) {
+    const float* src =
+        static_cast<const float*>(row_src<SCHEME, VARIANT>(p, fin, lane)) + size_t(tile) * TILE;
+    bulk_g2s(smem_u32(stage + lane * TILE), src, row_bytes, bar);
   }
 }
 
@@ -117,7 +120,7 @@ constexpr size_t tile_smem_bytes() {
           size_t(12) * TILE_MAX_ENTRIES) * sizeof(float) + 2 * sizeof(uint64_t);
 }
 
-template <int SCHEME, int VARIANT, bool FV>
+template <int SCHEME, int VARIANT, bool FV, bool NODES>
 __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __restrict__ fin,
                                                   float* __restrict__ fout) {
   using RW = TileRows<SCHEME, VARIANT>;
@@ -139,10 +142,10 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0) {
-    issue_tile<SCHEME, VARIANT>(p, fin, first, stage0, bar0);
+  if (tid < 32) {
+    issue_tile<SCHEME, VARIANT>(p, fin, first, stage0, bar0, tid);
     if (first + stride < p.NT)
-      issue_tile<SCHEME, VARIANT>(p, fin, first + stride, stage0 + RW::ROWS * TILE, bar1);
+      issue_tile<SCHEME, VARIANT>(p, fin, first + stride, stage0 + RW::ROWS * TILE, bar1, tid);
   }
 
   int it = 0;
@@ -155,18 +158,29 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
       // give up: report, let the copies still in flight land, return
       if (tid == 0) {
         atomicExch(p.status, STATUS_WAIT_TIMEOUT);
-        if (t + stride < p.NT) mbar_wait(s ? bar0 : bar1, ((it + 1) >> 1) & 1);
-        mbar_wait(bar, parity);
+        mbar_wait(bar, parity);                                 // this tile's copies
+        if (it == 0 && first + stride < p.NT) mbar_wait(bar1, 0);  // the pre-issued second tile
       }
       __syncthreads();
       return;
+    }
+    // every thread has finished the previous tile: refill its stage with
+    // the tile two iterations ahead of that one
+    if (it > 0 && tid < 32) {
+      const int tn = t + stride;
+      if (tn < p.NT) {
+        if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        issue_tile<SCHEME, VARIANT>(p, fin, tn, stage0 + (s ^ 1) * RW::ROWS * TILE, s ? bar0 : bar1, tid);
+      }
     }
     const float* S = stage0 + s * RW::ROWS * TILE;
     const int tile_start = t * TILE;
 
     // ---- phase A: boundary nodes needed by this tile
-    const int nb = __ldg(p.tn_ptr + t), nn = __ldg(p.tn_ptr + t + 1) - nb;
-    if (nn > 0) {
+    const int nb = NODES ? __ldg(p.tn_ptr + t) : 0;
+    const int nn = NODES ? __ldg(p.tn_ptr + t + 1) - nb : 0;
+    if (NODES && nn > 0) {
       const int eb = __ldg(p.te_ptr + t), ne = __ldg(p.te_ptr + t + 1) - eb;
       if (tid < ne) {
         const unsigned code = __ldg(p.te_cell + eb + tid);
@@ -283,12 +297,22 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
         const bool slot1 = (code & HF_SLOT1) != 0;
         float o[Q];
         if (code & HF_GHOST) {
-          const int la = __ldg(p.tgh_a + other), lb = __ldg(p.tgh_b + other);
           const float rg = __ldg(p.gh_r + other);
+          if (NODES) {
+            const int la = __ldg(p.tgh_a + other), lb = __ldg(p.tgh_b + other);
 #pragma unroll
-          for (int q = 0; q < Q; ++q) {
-            const float mq = (npdf[q * TILE_MAX_NODES + la] + npdf[q * TILE_MAX_NODES + lb]) / 2.0f;
-            o[q] = mq + (mq - f[q]) * rg;
+            for (int q = 0; q < Q; ++q) {
+              const float mq = (npdf[q * TILE_MAX_NODES + la] + npdf[q * TILE_MAX_NODES + lb]) / 2.0f;
+              o[q] = mq + (mq - f[q]) * rg;
+            }
+          } else {
+            const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+              const float mq = (__ldg(p.node_pdf + size_t(q) * p.Mp + a) +
+                                __ldg(p.node_pdf + size_t(q) * p.Mp + b)) / 2.0f;
+              o[q] = mq + (mq - f[q]) * rg;
+            }
           }
         } else {
           const unsigned lo = unsigned(other - tile_start);
@@ -330,20 +354,13 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
         fout[q * Np + i] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
     }
 
-    // ---- refill this stage with the tile two steps ahead
-    __syncthreads();
-    const int tn = t + 2 * stride;
-    if (tid == 0 && tn < p.NT) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue_tile<SCHEME, VARIANT>(p, fin, tn, stage0 + s * RW::ROWS * TILE, bar);
-    }
   }
 }
 
 namespace {
 
 // Grid = SMs x resident CTAs per SM, per instantiation and device.
-template <int S, int V, bool FV>
+template <int S, int V, bool FV, bool NODES>
 struct TileLaunch {
   static int grid[64];
 
@@ -354,37 +371,54 @@ struct TileLaunch {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     if (grid[dev] > 0) return cudaSuccess;
     constexpr size_t smem = tile_smem_bytes<S, V>();
-    e = cudaFuncSetAttribute(k_tile<S, V, FV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = cudaFuncSetAttribute(k_tile<S, V, FV, NODES>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    // the whole unified L1/shared array as shared memory: several CTAs per SM
+    e = cudaFuncSetAttribute(k_tile<S, V, FV, NODES>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             int(cudaSharedmemCarveoutMaxShared));
     if (e != cudaSuccess) return e;
     int sms = 0, per_sm = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<S, V, FV>, TILE, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<S, V, FV, NODES>, TILE, smem);
     if (e != cudaSuccess) return e;
     grid[dev] = sms * (per_sm > 0 ? per_sm : 1);
+    per_sm_[dev] = per_sm;
     return cudaSuccess;
   }
+  static int per_sm_[64];
 
   static cudaError_t launch(const DevPlan& p, const float* fin, float* fout, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || grid[dev] <= 0) return cudaErrorNotReady;
     const int g = grid[dev] < p.NT ? grid[dev] : p.NT;
-    k_tile<S, V, FV><<<g, TILE, tile_smem_bytes<S, V>(), st>>>(p, fin, fout);
+    k_tile<S, V, FV, NODES><<<g, TILE, tile_smem_bytes<S, V>(), st>>>(p, fin, fout);
     return cudaGetLastError();
   }
 };
 
-template <int S, int V, bool FV>
-int TileLaunch<S, V, FV>::grid[64] = {0};
+template <int S, int V, bool FV, bool NODES>
+int TileLaunch<S, V, FV, NODES>::grid[64] = {0};
+template <int S, int V, bool FV, bool NODES>
+int TileLaunch<S, V, FV, NODES>::per_sm_[64] = {0};
+
+template <bool NODES, class Fn>
+cudaError_t dispatch_n(const DevPlan& p, Fn&& fn) {
+  if (p.scheme == 0 && p.variant == 0)
+    return p.fv ? fn(TileLaunch<0, 0, true, NODES>{}) : fn(TileLaunch<0, 0, false, NODES>{});
+  if (p.scheme == 1 && p.variant == 0)
+    return p.fv ? fn(TileLaunch<1, 0, true, NODES>{}) : fn(TileLaunch<1, 0, false, NODES>{});
+  if (p.scheme == 0 && p.variant == 1)
+    return p.fv ? fn(TileLaunch<0, 1, true, NODES>{}) : fn(TileLaunch<0, 1, false, NODES>{});
+  if (p.scheme == 1 && p.variant == 1)
+    return p.fv ? fn(TileLaunch<1, 1, true, NODES>{}) : fn(TileLaunch<1, 1, false, NODES>{});
+  return cudaErrorInvalidValue;
+}
 
 template <class Fn>
 cudaError_t dispatch(const DevPlan& p, Fn&& fn) {
-  if (p.scheme == 0 && p.variant == 0) return p.fv ? fn(TileLaunch<0, 0, true>{}) : fn(TileLaunch<0, 0, false>{});
-  if (p.scheme == 1 && p.variant == 0) return p.fv ? fn(TileLaunch<1, 0, true>{}) : fn(TileLaunch<1, 0, false>{});
-  if (p.scheme == 0 && p.variant == 1) return p.fv ? fn(TileLaunch<0, 1, true>{}) : fn(TileLaunch<0, 1, false>{});
-  if (p.scheme == 1 && p.variant == 1) return p.fv ? fn(TileLaunch<1, 1, true>{}) : fn(TileLaunch<1, 1, false>{});
-  return cudaErrorInvalidValue;
+  return p.tile_nodes ? dispatch_n<true>(p, fn) : dispatch_n<false>(p, fn);
 }
 
 }  // namespace
@@ -392,6 +426,18 @@ cudaError_t dispatch(const DevPlan& p, Fn&& fn) {
 cudaError_t prepare_tile(const DevPlan& p) {
   if (p.K != 3) return cudaErrorInvalidValue;
   return dispatch(p, [](auto L) { return decltype(L)::prepare(); });
+}
+
+int tile_ctas_per_sm(const DevPlan& p) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 0;
+  int out = 0;
+  dispatch(p, [&](auto L) {
+    out = decltype(L)::per_sm_[dev];
+    return cudaSuccess;
+  });
+  return out;
 }
 
 cudaError_t launch_tile(const DevPlan& p, const float* fin, float* fout, cudaStream_t st) {

@@ -58,10 +58,11 @@ extern "C" {
 #define FVDBM_ORDER_MORTON 2 /* Z-order of cell_xy (needs cell_xy) */
 
 /* Kernel family for the step. */
-#define FVDBM_KERNEL_AUTO 0   /* tile when the mesh allows it, else fused, else staged */
-#define FVDBM_KERNEL_STAGED 1 /* node BC + face flux + cell gather (3 kernels) */
-#define FVDBM_KERNEL_FUSED 2  /* node BC + fused cell kernel (2 kernels) */
-#define FVDBM_KERNEL_TILE 3   /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
+#define FVDBM_KERNEL_AUTO 0       /* fastest family the mesh allows */
+#define FVDBM_KERNEL_STAGED 1     /* node BC + face flux + cell gather (3 kernels) */
+#define FVDBM_KERNEL_FUSED 2      /* node BC + fused cell kernel (2 kernels) */
+#define FVDBM_KERNEL_TILE 3       /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
+#define FVDBM_KERNEL_TILE_SPLIT 4 /* node BC kernel + persistent tile kernel (2 kernels) */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {
@@ -109,6 +110,7 @@ typedef struct fvdbm_info {
   int32_t kernel;           /* family actually used */
   int32_t launches_per_step;
   int32_t padded_cells;     /* row stride of the [9][Np] pdf */
+  int32_t ctas_per_sm;      /* resident CTAs per SM of the tile kernel (0 if unused) */
   int32_t const_division;   /* 1: divisions by the lattice constants use the
                                known-divisor form, verified on this device to
                                equal IEEE division for every float32 dividend */
