@@ -12,15 +12,6 @@
 
 namespace fvdbm {
 
-// [9][Np] device order -> [N][9] reference order.
-__global__ void k_soa_to_aos(const float* __restrict__ src, float* __restrict__ dst,
-                             const int* __restrict__ cell_new, int N, int Np, int rows) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= N) return;
-  const int d = cell_new[c];
-  for (int q = 0; q < rows; ++q) dst[size_t(c) * rows + q] = src[size_t(q) * Np + d];
-}
-
 namespace {
 
 std::mutex g_err_mu;
@@ -338,14 +329,9 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   UP(fscale, hp.fscale);
   UP(cf_face, hp.cf_face);
   UP(cf_sign, hp.cf_sign);
+  p.hrows = hp.hrows;
   if (h->fused) {
-    UP(hf_code, hp.hf_code);
-    UP(hf_nx, hp.hf_nx);
-    UP(hf_ny, hp.hf_ny);
-    UP(hf_L, hp.hf_L);
-    UP(hf_r, hp.hf_r);
-    UP(hf_D2, hp.hf_D2);
-    UP(hf_scale, hp.hf_scale);
+    UP(hf, hp.hf);
     UP(gh_a, hp.gh_a);
     UP(gh_b, hp.gh_b);
     UP(gh_r, hp.gh_r);
@@ -356,6 +342,8 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   UP(nd_cell, hp.nd_cell);
   UP(nd_w, hp.nd_w);
   UP(nd_sumw, hp.nd_sumw);
+  UP(nb_ptr, hp.nb_ptr);
+  p.NB = hp.nb_ptr.empty() ? 0 : int(hp.nb_ptr.size()) - 1;
   UP(inv_area, hp.inv_area);
   p.NT = hp.NT;
   if (h->tile) {
@@ -428,7 +416,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
   CK(cudaSetDevice(h->device));
   if (cell_pdf && hp.N > 0) {
     CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(Q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
-    CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, hp.Np, h->stream));
+    CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream));
   }
   if (node_pdf || node_rho || node_vel) {
     if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(Q) * hp.P * 4);
@@ -520,10 +508,8 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
   const int N = hp.N;
-  const int tb = 256, nb = (N + tb - 1) / tb;
   if (pdf && N > 0) {
-    k_soa_to_aos<<<nb, tb, 0, h->stream>>>(h->f[h->cur], h->stage, h->d_cell_new, N, hp.Np, Q);
-    CK(cudaGetLastError());
+    CK(launch_gather_cells(h->f[h->cur], h->stage, h->d_cell_new, N, h->stream));
     CK(cudaMemcpyAsync(pdf, h->stage, size_t(Q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
   }
@@ -542,20 +528,17 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
       float* me = h->mac + size_t(3) * hp.Np;
       CK(launch_macros(h->dp, h->f[h->cur ^ 1], mr, mv, me, h->stream));
       if (rho) {
-        k_soa_to_aos<<<nb, tb, 0, h->stream>>>(mr, h->stage, h->d_cell_new, N, hp.Np, 1);
-        CK(cudaGetLastError());
+        CK(launch_soa_to_aos(mr, h->stage, h->d_cell_new, N, hp.Np, 1, h->stream));
         CK(cudaMemcpyAsync(rho, h->stage, size_t(N) * 4, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
       }
       if (vel) {
-        k_soa_to_aos<<<nb, tb, 0, h->stream>>>(mv, h->stage, h->d_cell_new, N, hp.Np, 2);
-        CK(cudaGetLastError());
+        CK(launch_soa_to_aos(mv, h->stage, h->d_cell_new, N, hp.Np, 2, h->stream));
         CK(cudaMemcpyAsync(vel, h->stage, size_t(2) * N * 4, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
       }
       if (pdf_eq) {
-        k_soa_to_aos<<<nb, tb, 0, h->stream>>>(me, h->stage, h->d_cell_new, N, hp.Np, Q);
-        CK(cudaGetLastError());
+        CK(launch_gather_cells(me, h->stage, h->d_cell_new, N, h->stream));
         CK(cudaMemcpyAsync(pdf_eq, h->stage, size_t(Q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
       }

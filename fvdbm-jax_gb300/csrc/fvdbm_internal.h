@@ -28,6 +28,20 @@ constexpr int TILE = 256;
 constexpr int TILE_MAX_NODES = 128;    // nodes evaluated per tile
 constexpr int TILE_MAX_ENTRIES = 256;  // node-stencil cells per tile
 constexpr int TN_OWNER = 1 << 4;       // tn_kind flag: this tile writes the node state
+constexpr int NODE_BLOCK_ENTRIES = 128; // node kernel: entries (= threads) per block
+
+// rows of the half-face array for K face slots
+struct HfRows {
+  int K, scheme, variant;
+  __host__ __device__ constexpr int code(int k) const { return k; }
+  __host__ __device__ constexpr int nx(int k) const { return K + k; }
+  __host__ __device__ constexpr int ny(int k) const { return 2 * K + k; }
+  __host__ __device__ constexpr int ls(int k) const { return 3 * K + k; }
+  __host__ __device__ constexpr int r(int k) const { return 4 * K + k; }
+  __host__ __device__ constexpr int d2(int k) const { return (scheme == 1 ? 5 : 4) * K + k; }
+  __host__ __device__ constexpr int sc(int k) const { return (scheme == 1 ? 6 : 4) * K + k; }
+  __host__ __device__ constexpr int rows() const { return (4 + (scheme == 1 ? 2 : 0) + (variant == 1 ? 1 : 0)) * K; }
+};
 
 // Node-cell entry: cell index (device numbering); bit 31 marks an entry whose
 // reference index was -1 (its rho/vel gather wraps to the last cell but its
@@ -63,11 +77,16 @@ struct HostPlan {
   std::vector<int32_t> cf_face;
   std::vector<float> cf_sign;
 
-  // fused half faces: [K][Np]
-  std::vector<int32_t> hf_code;
-  std::vector<float> hf_nx, hf_ny, hf_L, hf_r, hf_D2, hf_scale;  // hf_L holds L*sigma
+  // fused half faces, AoSoA [Np/32][hrows][32] of 32-bit words; rows are
+  // code (K), nx (K), ny (K), L*sigma (K), then d0/(d0+d1) (K), 2(d0+d1) (K)
+  // for Lax-Wendroff, then the stencil scale (K) for the cos variant
+  int hrows = 0;
+  std::vector<uint32_t> hf;
   std::vector<int32_t> gh_a, gh_b;
   std::vector<float> gh_r;
+  // node blocks of the node kernel: contiguous computed nodes with at most
+  // NODE_BLOCK_ENTRIES stencil entries each
+  std::vector<int32_t> nb_ptr;
 
   // nodes on the device: computed (type 1/2) first, then frozen ghost ends
   int M = 0, Mc = 0, Mp = 0;
@@ -130,14 +149,9 @@ struct DevPlan {
   const float* fscale;
   const int* cf_face;
   const float* cf_sign;
-  // fused half faces
-  const int* hf_code;
-  const float* hf_nx;
-  const float* hf_ny;
-  const float* hf_L;
-  const float* hf_r;
-  const float* hf_D2;
-  const float* hf_scale;
+  // fused half faces (AoSoA, hrows rows)
+  const unsigned* hf;
+  int hrows;
   const int* gh_a;
   const int* gh_b;
   const float* gh_r;
@@ -148,6 +162,8 @@ struct DevPlan {
   const unsigned* nd_cell;
   const float* nd_w;
   const float* nd_sumw;
+  const int* nb_ptr;  // node blocks
+  int NB;
   float* node_pdf;  // [9][Mp]
   float* node_rho;  // [Mp]
   float* node_vel;  // [2][Mp]
@@ -191,7 +207,13 @@ cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* v
 // *bad must be zeroed and *example set to 0xFFFFFFFF.
 cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsigned* example,
                               cudaStream_t s);
-cudaError_t launch_scatter_cells(const float* src_aos, float* dst_soa, const int* cell_new, int N,
-                                 int Np, cudaStream_t s);
+// [N][9] reference order <-> AoSoA device order (cell_new: reference -> device)
+cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* cell_new, int N,
+                                 cudaStream_t s);
+cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
+                                cudaStream_t s);
+// SoA [rows][Np] device order -> [N][rows] reference order
+cudaError_t launch_soa_to_aos(const float* src, float* dst, const int* cell_new, int N, int Np,
+                              int rows, cudaStream_t s);
 
 }  // namespace fvdbm

@@ -23,6 +23,18 @@ static __constant__ float c_W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (f
 
 __device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
 
+// Cell arrays are AoSoA: blocks of 32 cells, [block][row][32].  A cell's
+// row r sits at cell_base(i) + r*32, a constant offset from one base.
+__device__ __forceinline__ size_t cell_base(int i, int rows) {
+  return size_t(i >> 5) * size_t(rows * 32) + size_t(i & 31);
+}
+
+__device__ __forceinline__ void load_cell(const float* __restrict__ f, int c, float out[Q]) {
+  const float* b = f + cell_base(c, Q);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) out[q] = __ldg(b + q * 32);
+}
+
 // Correctly rounded x/y for a divisor known in advance.  With zr = RN(1/y):
 // q0 = RN(x*zr) is within 1.5 ulp of x/y; one correction
 // q1 = RN(q0 + RN(x - q0*y)*zr) (remainder exact through an FMA) makes it
@@ -127,21 +139,48 @@ __device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, 
   uy = my / r;
 }
 
+// x == 0 or 2^-50 <= |x| <= 2^50: then x, x*x and sums of two such squares
+// are dividends for which the known-divisor division is exact (the
+// exhaustive check covers |x| >= 2^-100 with normal quotients).
+__device__ __forceinline__ bool cdiv_domain(float x) {
+  const float a = fabsf(x);
+  return (a >= 0x1p-50f && a <= 0x1p50f) || x == 0.0f;
+}
+
 // feq_q = (W_q rho) * (((1 + a_q/C^2) + a_q^2/(2C^4)) - u.u/(2C^2)).
 // With finite u: a_3 = -a_1, a_4 = -a_2, a_7 = -a_5, a_8 = -a_6 exactly, and
-// a_0 = +-0 gives s_0 = 1 - u.u/(2C^2).
+// a_0 = +-0 gives s_0 = 1 - u.u/(2C^2).  One range check per call decides
+// whether all nine divisions take the three-operation form.
 __device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPlan& p, float out[Q]) {
   if (!(finite(ux) && finite(uy))) {
     feq9_literal(rho, ux, uy, p, out);
     return;
   }
   const float uu = ux * ux + uy * uy;
-  const float t = cdiv(uu, p.d_c2x2);
   const float a5 = ux + uy, a6 = uy - ux;
-  const float x1 = cdiv(ux, p.d_c2), y1 = cdiv(ux * ux, p.d_c4x2);
-  const float x2 = cdiv(uy, p.d_c2), y2 = cdiv(uy * uy, p.d_c4x2);
-  const float x5 = cdiv(a5, p.d_c2), y5 = cdiv(a5 * a5, p.d_c4x2);
-  const float x6 = cdiv(a6, p.d_c2), y6 = cdiv(a6 * a6, p.d_c4x2);
+  float t, x1, y1, x2, y2, x5, y5, x6, y6;
+  if (p.d_c2.ok && p.d_c4x2.ok && p.d_c2x2.ok && cdiv_domain(ux) && cdiv_domain(uy) &&
+      cdiv_domain(a5) && cdiv_domain(a6)) {
+    t = cdiv_fast(uu, p.d_c2x2.y, p.d_c2x2.zr);
+    x1 = cdiv_fast(ux, p.d_c2.y, p.d_c2.zr);
+    y1 = cdiv_fast(ux * ux, p.d_c4x2.y, p.d_c4x2.zr);
+    x2 = cdiv_fast(uy, p.d_c2.y, p.d_c2.zr);
+    y2 = cdiv_fast(uy * uy, p.d_c4x2.y, p.d_c4x2.zr);
+    x5 = cdiv_fast(a5, p.d_c2.y, p.d_c2.zr);
+    y5 = cdiv_fast(a5 * a5, p.d_c4x2.y, p.d_c4x2.zr);
+    x6 = cdiv_fast(a6, p.d_c2.y, p.d_c2.zr);
+    y6 = cdiv_fast(a6 * a6, p.d_c4x2.y, p.d_c4x2.zr);
+  } else {
+    t = cdiv(uu, p.d_c2x2);
+    x1 = cdiv(ux, p.d_c2);
+    y1 = cdiv(ux * ux, p.d_c4x2);
+    x2 = cdiv(uy, p.d_c2);
+    y2 = cdiv(uy * uy, p.d_c4x2);
+    x5 = cdiv(a5, p.d_c2);
+    y5 = cdiv(a5 * a5, p.d_c4x2);
+    x6 = cdiv(a6, p.d_c2);
+    y6 = cdiv(a6 * a6, p.d_c4x2);
+  }
   float s[Q];
   s[0] = 1.0f - t;
   s[1] = ((1.0f + x1) + y1) - t;
@@ -154,6 +193,30 @@ __device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPla
   s[8] = ((1.0f - x6) + y6) - t;
 #pragma unroll
   for (int q = 0; q < Q; ++q) out[q] = (c_W[q] * rho) * s[q];
+}
+
+// One component q of feq9, bitwise equal to feq9(...)[q].
+__device__ __forceinline__ float feq_one(float rho, float ux, float uy, int q, const DevPlan& p) {
+  if (!(finite(ux) && finite(uy))) {
+    float a[Q];
+    xi_dot_literal(ux, uy, a);
+    const float uu = ux * ux + uy * uy;
+    float s = 1.0f + a[q] / p.c2;
+    s = s + (a[q] * a[q]) / p.c4x2;
+    s = s - uu / p.c2x2;
+    return (c_W[q] * rho) * s;
+  }
+  const float uu = ux * ux + uy * uy;
+  const float t = cdiv(uu, p.d_c2x2);
+  if (q == 0) return (c_W[0] * rho) * (1.0f - t);
+  // a_q for q = 1..8 in the symmetric form: (+-) of ux, uy, ux+uy, uy-ux
+  const int base = (q <= 4) ? ((q - 1) & 1) : 2 + ((q - 5) & 1);
+  const float ab = base == 0 ? ux : base == 1 ? uy : base == 2 ? ux + uy : uy - ux;
+  const bool neg = (q == 3 || q == 4 || q == 7 || q == 8);
+  const float x = cdiv(ab, p.d_c2);
+  const float y = cdiv(ab * ab, p.d_c4x2);
+  const float s = ((neg ? 1.0f - x : 1.0f + x) + y) - t;
+  return (c_W[q] * rho) * s;
 }
 
 // v_q = xi_q . n (src/containers.py:235); symmetric form for finite n

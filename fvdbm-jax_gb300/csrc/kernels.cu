@@ -2,108 +2,95 @@
 // kernel, the staged face/gather pair, read-back helpers and the division
 // self-check.  Arithmetic helpers live in fvdbm_math.cuh.
 //
-// Layout: cell pdfs are SoA [9][Np] float32 in device (renumbered) cell
-// order; node state is SoA [9][Mp]; per-cell face slots are SoA [K][Np].
+// Layout: cell pdfs are AoSoA [Np/32][9][32] float32 in device (renumbered)
+// cell order; the fused kernel's per-cell face slots are AoSoA
+// [Np/32][hrows][32]; node state is SoA [9][Mp].
 #include "fvdbm_math.cuh"
 
 namespace fvdbm {
 
 // ---------------------------------------------------------------------------
-// Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  One group of
-// 8 lanes per node: each lane evaluates one of the node's cells (macros, feq,
-// the IDW products), then every lane folds the products in the reference's
-// entry order through shuffles.  Velocity nodes (type 1) take rho =
-// IDW(cell rho); density nodes (type 2) take u = IDW(cell u); both set pdf =
-// feq(rho, u) + IDW(f - feq).
-constexpr int NODE_LANES = 8;
-
-__global__ void __launch_bounds__(128) k_nodes(DevPlan p, const float* __restrict__ f) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = tid / NODE_LANES;
-  const int lane = threadIdx.x % NODE_LANES;
-  if (m >= p.Mc) return;  // whole 8-lane group leaves together
-  const unsigned mask = 0xFFu << (threadIdx.x & 24);
-  const int b = __ldg(p.nd_ptr + m), e = __ldg(p.nd_ptr + m + 1);
-  const size_t Np = p.Np;
-  float ar = 0.0f, ax = 0.0f, ay = 0.0f, an[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) an[q] = 0.0f;
-  bool first = true;
-  for (int base = b; base < e; base += NODE_LANES) {
-    const int j = base + lane;
-    float xr = 0.0f, xx = 0.0f, xy = 0.0f, xn[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) xn[q] = 0.0f;
-    if (j < e) {
-      const unsigned code = __ldg(p.nd_cell + j);
-      const int c = int(code & ~ND_NEQ_ZERO);
-      const float w = __ldg(p.nd_w + j);
-      float fc[Q], eq[Q];
-#pragma unroll
-      for (int q = 0; q < Q; ++q) fc[q] = __ldg(f + q * Np + c);
-      float rho, ux, uy;
-      macros(fc, rho, ux, uy);
-      feq9(rho, ux, uy, p, eq);
-      const bool zero = (code & ND_NEQ_ZERO) != 0;
-      xr = rho * w;
-      xx = ux * w;
-      xy = uy * w;
-#pragma unroll
-      for (int q = 0; q < Q; ++q) xn[q] = (zero ? 0.0f : fc[q] - eq[q]) * w;
-    }
-    const int cnt = min(NODE_LANES, e - base);
-    for (int t = 0; t < cnt; ++t) {
-      const float vr = __shfl_sync(mask, xr, t, NODE_LANES);
-      const float vx = __shfl_sync(mask, xx, t, NODE_LANES);
-      const float vy = __shfl_sync(mask, xy, t, NODE_LANES);
-      if (first) {
-        ar = vr;
-        ax = vx;
-        ay = vy;
-      } else {
-        ar = ar + vr;
-        ax = ax + vx;
-        ay = ay + vy;
-      }
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const float vn = __shfl_sync(mask, xn[q], t, NODE_LANES);
-        an[q] = first ? vn : an[q] + vn;
-      }
-      first = false;
-    }
-  }
-  if (__ldg(p.nd_npad + m) > 0) {
-    // padded (-1, weight 0) entries gather the last cell: rho*0, u*0
-    float fc[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) fc[q] = __ldg(f + q * Np + p.last_cell);
+// Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  A block holds
+// whole nodes with at most NODE_BLOCK_ENTRIES stencil entries:
+//   1. one thread per entry: that cell's macros, feq and the IDW products
+//      rho*w, u*w, (f - feq)*w (utils/utils.py:34-60);
+//   2. one thread per (node, component): the ordered fold over the node's
+//      entries (the reference's sum order);
+//   3. one thread per (node, q): velocity nodes (type 1) take rho =
+//      IDW(cell rho), density nodes (type 2) take u = IDW(cell u);
+//      pdf_q = feq_q(rho, u) + IDW(f - feq)_q.
+__global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const float* __restrict__ f) {
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float fold[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  const int n0 = __ldg(p.nb_ptr + blockIdx.x), n1 = __ldg(p.nb_ptr + blockIdx.x + 1);
+  const int nn = n1 - n0;
+  const int e0 = __ldg(p.nd_ptr + n0), ne = __ldg(p.nd_ptr + n1) - e0;
+  const int tid = threadIdx.x;
+  if (tid < ne) {
+    const unsigned code = __ldg(p.nd_cell + e0 + tid);
+    const float w = __ldg(p.nd_w + e0 + tid);
+    float fc[Q], eq[Q];
+    load_cell(f, int(code & ~ND_NEQ_ZERO), fc);
     float rho, ux, uy;
     macros(fc, rho, ux, uy);
-    ar = first ? rho * 0.0f : ar + rho * 0.0f;
-    ax = first ? ux * 0.0f : ax + ux * 0.0f;
-    ay = first ? uy * 0.0f : ay + uy * 0.0f;
-  }
-  if (lane != 0) return;
-  const float sw = __ldg(p.nd_sumw + m);
-  const int type = __ldg(p.nd_type + m);
-  float rho_p, ux_p, uy_p;
-  if (type == 1) {
-    rho_p = ar / sw;
-    ux_p = p.node_vel[m];
-    uy_p = p.node_vel[p.Mp + m];
-    p.node_rho[m] = rho_p;
-  } else {
-    rho_p = p.node_rho[m];
-    ux_p = ax / sw;
-    uy_p = ay / sw;
-    p.node_vel[m] = ux_p;
-    p.node_vel[p.Mp + m] = uy_p;
-  }
-  float eqn[Q];
-  feq9(rho_p, ux_p, uy_p, p, eqn);
+    feq9(rho, ux, uy, p, eq);
+    const bool zero = (code & ND_NEQ_ZERO) != 0;
+    prod[0][tid] = rho * w;
+    prod[1][tid] = ux * w;
+    prod[2][tid] = uy * w;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) p.node_pdf[size_t(q) * p.Mp + m] = eqn[q] + an[q] / sw;
+    for (int q = 0; q < Q; ++q) prod[3 + q][tid] = (zero ? 0.0f : fc[q] - eq[q]) * w;
+  }
+  if (tid == NODE_BLOCK_ENTRIES - 1) {
+    // padded (-1, weight 0) entries gather the last cell
+    float fc[Q];
+    load_cell(f, p.last_cell, fc);
+    float rho, ux, uy;
+    macros(fc, rho, ux, uy);
+    lastm[0] = rho;
+    lastm[1] = ux;
+    lastm[2] = uy;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nn * 12; idx += NODE_BLOCK_ENTRIES) {
+    const int j = idx / 12, r = idx % 12;
+    const int m = n0 + j;
+    const int b = __ldg(p.nd_ptr + m) - e0, cnt = __ldg(p.nd_ptr + m + 1) - e0 - b;
+    float acc = 0.0f;
+    for (int k = 0; k < cnt; ++k) acc = k ? acc + prod[r][b + k] : prod[r][b];
+    if (r < 3 && __ldg(p.nd_npad + m) > 0) {
+      const float z = lastm[r] * 0.0f;
+      acc = cnt ? acc + z : z;
+    }
+    fold[r][j] = acc;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nn * Q; idx += NODE_BLOCK_ENTRIES) {
+    const int j = idx / Q, q = idx % Q;
+    const int m = n0 + j;
+    const float sw = __ldg(p.nd_sumw + m);
+    const int type = __ldg(p.nd_type + m);
+    float rho_p, ux_p, uy_p;
+    if (type == 1) {
+      rho_p = fold[0][j] / sw;
+      ux_p = p.node_vel[m];
+      uy_p = p.node_vel[p.Mp + m];
+    } else {
+      rho_p = p.node_rho[m];
+      ux_p = fold[1][j] / sw;
+      uy_p = fold[2][j] / sw;
+    }
+    p.node_pdf[size_t(q) * p.Mp + m] = feq_one(rho_p, ux_p, uy_p, q, p) + fold[3 + q][j] / sw;
+    if (q == 0) {
+      if (type == 1) {
+        p.node_rho[m] = rho_p;
+      } else {
+        p.node_vel[m] = ux_p;
+        p.node_vel[p.Mp + m] = uy_p;
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -112,12 +99,14 @@ __global__ void __launch_bounds__(128) k_nodes(DevPlan p, const float* __restric
 // bit-identical fluxes without a flux array or atomics), the signed flux sum
 // and the BGK/explicit-Euler update (src/containers.py:107-121).
 template <int SCHEME, int VARIANT, bool FIRST>
-__device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin, size_t Np,
-                                           int i, int k, const float f[Q], float acc[Q]) {
-  const size_t s = size_t(k) * Np + i;
-  const int code = __ldg(p.hf_code + s);
-  const float nx = __ldg(p.hf_nx + s), ny = __ldg(p.hf_ny + s);
-  const float Ls = __ldg(p.hf_L + s);  // L * sigma
+__device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin,
+                                           const unsigned* __restrict__ hb, int k, const float f[Q],
+                                           float acc[Q]) {
+  const HfRows HR{3, SCHEME, VARIANT};
+  const int code = int(__ldg(hb + HR.code(k) * 32));
+  const float nx = __uint_as_float(__ldg(hb + HR.nx(k) * 32));
+  const float ny = __uint_as_float(__ldg(hb + HR.ny(k) * 32));
+  const float Ls = __uint_as_float(__ldg(hb + HR.ls(k) * 32));  // L * sigma
   const int other = code >> HF_SHIFT;
   const bool slot1 = (code & HF_SLOT1) != 0;
   float o[Q];
@@ -133,14 +122,15 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
       o[q] = mq + (mq - f[q]) * rg;
     }
   } else {
-#pragma unroll
-    for (int q = 0; q < Q; ++q) o[q] = __ldg(fin + q * Np + other);
+    load_cell(fin, other, o);
   }
   float v[Q];
   xi_dot_n(nx, ny, p.finite_n != 0, v);
   float w[Q];
-  if (SCHEME == 1) lw_interp(v, __ldg(p.hf_r + s), __ldg(p.hf_D2 + s), p.dt, p.finite_n != 0, w);
-  const float scale = (VARIANT == 1) ? __ldg(p.hf_scale + s) : 1.0f;
+  if (SCHEME == 1)
+    lw_interp(v, __uint_as_float(__ldg(hb + HR.r(k) * 32)), __uint_as_float(__ldg(hb + HR.d2(k) * 32)),
+              p.dt, p.finite_n != 0, w);
+  const float scale = (VARIANT == 1) ? __uint_as_float(__ldg(hb + HR.sc(k) * 32)) : 1.0f;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     float phi;
@@ -157,40 +147,43 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
   }
 }
 
-template <int SCHEME, int VARIANT, bool FV, int KT>
+__device__ __forceinline__ void prefetch_l2(const void* ptr, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
+}
+
+template <int SCHEME, int VARIANT, bool FV>
 __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restrict__ fin,
-                                               float* __restrict__ fout) {
+                                               float* __restrict__ fout, int prefetch_blocks) {
+  constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+  // the block about one wave ahead streams into L2 while this one computes
+  if (threadIdx.x == 0 && prefetch_blocks > 0) {
+    const int ahead = blockIdx.x + prefetch_blocks;
+    if (ahead < int(gridDim.x)) {
+      const size_t c0 = size_t(ahead) * 256;
+      prefetch_l2(fin + c0 * Q, 256 * Q * sizeof(float));
+      prefetch_l2(p.hf + c0 * HROWS, 256 * HROWS * sizeof(unsigned));
+    }
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.N) return;
-  const size_t Np = p.Np;
   float f[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) f[q] = __ldg(fin + q * Np + i);
+  load_cell(fin, i, f);
   float rho, ux, uy, eq[Q];
   macros(f, rho, ux, uy);
   feq9(rho, ux, uy, p, eq);
-
+  const unsigned* hb = p.hf + cell_base(i, HROWS);
   float acc[Q];
-  const int K = KT > 0 ? KT : p.K;
-  if (K == 0) {
-#pragma unroll
-    for (int q = 0; q < Q; ++q) acc[q] = 0.0f;
-  } else {
-    fused_face<SCHEME, VARIANT, true>(p, fin, Np, i, 0, f, acc);
-    if (KT > 0) {
-#pragma unroll
-      for (int k = 1; k < KT; ++k) fused_face<SCHEME, VARIANT, false>(p, fin, Np, i, k, f, acc);
-    } else {
-      for (int k = 1; k < K; ++k) fused_face<SCHEME, VARIANT, false>(p, fin, Np, i, k, f, acc);
-    }
-  }
+  fused_face<SCHEME, VARIANT, true>(p, fin, hb, 0, f, acc);
+  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 1, f, acc);
+  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 2, f, acc);
   if (FV) {
     const float ia = __ldg(p.inv_area + i);
 #pragma unroll
     for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
   }
+  float* o = fout + cell_base(i, Q);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) fout[q * Np + i] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+  for (int q = 0; q < Q; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
 }
 
 // ---------------------------------------------------------------------------
@@ -201,15 +194,11 @@ __global__ void __launch_bounds__(256) k_face(DevPlan p, const float* __restrict
                                               float* __restrict__ flux) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.F) return;
-  const size_t Np = p.Np;
   const int s0 = p.fs0[j], s1 = p.fs1[j];
   float lf[Q], rf[Q];
   if (s0 >= 0 && s1 >= 0) {
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      lf[q] = __ldg(f + q * Np + s0);
-      rf[q] = __ldg(f + q * Np + s1);
-    }
+    load_cell(f, s0, lf);
+    load_cell(f, s1, rf);
   } else {
     const int a = p.fna[j], b = p.fnb[j];
     float mq[Q];
@@ -217,22 +206,22 @@ __global__ void __launch_bounds__(256) k_face(DevPlan p, const float* __restrict
     for (int q = 0; q < Q; ++q)
       mq[q] = (p.node_pdf[size_t(q) * p.Mp + a] + p.node_pdf[size_t(q) * p.Mp + b]) / 2.0f;
     if (s0 >= 0) {
-#pragma unroll
-      for (int q = 0; q < Q; ++q) lf[q] = __ldg(f + q * Np + s0);
+      load_cell(f, s0, lf);
     } else {
-      const int kn = p.fkl[j];
+      float kf[Q];
+      load_cell(f, p.fkl[j], kf);
       const float rg = p.frl[j];
 #pragma unroll
-      for (int q = 0; q < Q; ++q) lf[q] = mq[q] + (mq[q] - __ldg(f + q * Np + kn)) * rg;
+      for (int q = 0; q < Q; ++q) lf[q] = mq[q] + (mq[q] - kf[q]) * rg;
     }
     if (s1 >= 0) {
-#pragma unroll
-      for (int q = 0; q < Q; ++q) rf[q] = __ldg(f + q * Np + s1);
+      load_cell(f, s1, rf);
     } else {
-      const int kn = p.fkr[j];
+      float kf[Q];
+      load_cell(f, p.fkr[j], kf);
       const float rg = p.frr[j];
 #pragma unroll
-      for (int q = 0; q < Q; ++q) rf[q] = mq[q] + (mq[q] - __ldg(f + q * Np + kn)) * rg;
+      for (int q = 0; q < Q; ++q) rf[q] = mq[q] + (mq[q] - kf[q]) * rg;
     }
   }
   float v[Q], w[Q];
@@ -260,8 +249,7 @@ __global__ void __launch_bounds__(256) k_gather(DevPlan p, const float* __restri
   if (i >= p.N) return;
   const size_t Np = p.Np;
   float f[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) f[q] = __ldg(fin + q * Np + i);
+  load_cell(fin, i, f);
   float rho, ux, uy, eq[Q];
   macros(f, rho, ux, uy);
   feq9(rho, ux, uy, p, eq);
@@ -282,39 +270,58 @@ __global__ void __launch_bounds__(256) k_gather(DevPlan p, const float* __restri
 #pragma unroll
     for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
   }
+  float* o = fout + cell_base(i, Q);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) fout[q * Np + i] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+  for (int q = 0; q < Q; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
 }
 
 // Cells.rho/vel/pdf_eq of a pdf buffer (Cells.calc_macros/calc_eqs,
-// src/containers.py:93-105).  rho [Np], vel [2][Np], feq [9][Np].
+// src/containers.py:93-105).  rho [Np], vel [2][Np] (SoA), feq AoSoA like f.
 __global__ void __launch_bounds__(256) k_macros(DevPlan p, const float* __restrict__ f,
                                                 float* __restrict__ rho_o, float* __restrict__ vel_o,
                                                 float* __restrict__ feq_o) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.N) return;
-  const size_t Np = p.Np;
   float fc[Q], eq[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) fc[q] = f[q * Np + i];
+  load_cell(f, i, fc);
   float rho, ux, uy;
   macros(fc, rho, ux, uy);
   feq9(rho, ux, uy, p, eq);
   rho_o[i] = rho;
   vel_o[i] = ux;
-  vel_o[Np + i] = uy;
+  vel_o[size_t(p.Np) + i] = uy;
+  float* o = feq_o + cell_base(i, Q);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) feq_o[q * Np + i] = eq[q];
+  for (int q = 0; q < Q; ++q) o[q * 32] = eq[q];
 }
 
-// [N][9] reference order -> [9][Np] device order.
-__global__ void k_aos_to_soa(const float* __restrict__ src, float* __restrict__ dst,
-                             const int* __restrict__ cell_new, int N, int Np) {
+// [N][9] reference order -> AoSoA device order.
+__global__ void k_aos_to_cells(const float* __restrict__ src, float* __restrict__ dst,
+                               const int* __restrict__ cell_new, int N) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  float* o = dst + cell_base(cell_new[c], Q);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) o[q * 32] = src[size_t(c) * Q + q];
+}
+
+// AoSoA device order -> [N][9] reference order.
+__global__ void k_cells_to_aos(const float* __restrict__ src, float* __restrict__ dst,
+                               const int* __restrict__ cell_new, int N) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const float* b = src + cell_base(cell_new[c], Q);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) dst[size_t(c) * Q + q] = b[q * 32];
+}
+
+// SoA [rows][Np] device order -> [N][rows] reference order.
+__global__ void k_soa_to_aos(const float* __restrict__ src, float* __restrict__ dst,
+                             const int* __restrict__ cell_new, int N, int Np, int rows) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= N) return;
   const int d = cell_new[c];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) dst[size_t(q) * Np + d] = src[size_t(c) * Q + q];
+  for (int q = 0; q < rows; ++q) dst[size_t(c) * rows + q] = src[size_t(q) * Np + d];
 }
 
 // Exhaustive check of cdiv against IEEE division: every float32 bit pattern
@@ -350,25 +357,33 @@ __global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, unsigned 
 static inline int blocks(long long n, int t) { return int((n + t - 1) / t); }
 
 cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s) {
-  if (p.Mc == 0) return cudaSuccess;
-  k_nodes<<<blocks((long long)p.Mc * NODE_LANES, 128), 128, 0, s>>>(p, f);
+  if (p.NB == 0) return cudaSuccess;
+  k_nodes<<<p.NB, NODE_BLOCK_ENTRIES, 0, s>>>(p, f);
   return cudaGetLastError();
+}
+
+static int fused_prefetch_blocks() {
+  static int cached = -1;
+  if (cached < 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cached = sms * 4;  // about one wave of 256-thread blocks
+  }
+  return cached;
 }
 
 template <int S, int V>
 static void fused_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
   const int g = blocks(p.N, 256);
-  if (p.K == 3) {
-    if (p.fv) k_fused<S, V, true, 3><<<g, 256, 0, s>>>(p, fin, fout);
-    else k_fused<S, V, false, 3><<<g, 256, 0, s>>>(p, fin, fout);
-  } else {
-    if (p.fv) k_fused<S, V, true, 0><<<g, 256, 0, s>>>(p, fin, fout);
-    else k_fused<S, V, false, 0><<<g, 256, 0, s>>>(p, fin, fout);
-  }
+  const int pf = fused_prefetch_blocks();
+  if (p.fv) k_fused<S, V, true><<<g, 256, 0, s>>>(p, fin, fout, pf);
+  else k_fused<S, V, false><<<g, 256, 0, s>>>(p, fin, fout, pf);
 }
 
 cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
   if (p.N == 0) return cudaSuccess;
+  if (p.K != 3) return cudaErrorInvalidValue;
   if (p.scheme == 0 && p.variant == 0) fused_dispatch<0, 0>(p, fin, fout, s);
   else if (p.scheme == 1 && p.variant == 0) fused_dispatch<1, 0>(p, fin, fout, s);
   else if (p.scheme == 0 && p.variant == 1) fused_dispatch<0, 1>(p, fin, fout, s);
@@ -416,10 +431,24 @@ cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsign
   return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_cells(const float* src_aos, float* dst_soa, const int* cell_new, int N,
-                                 int Np, cudaStream_t s) {
+cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* cell_new, int N,
+                                 cudaStream_t s) {
   if (N == 0) return cudaSuccess;
-  k_aos_to_soa<<<blocks(N, 256), 256, 0, s>>>(src_aos, dst_soa, cell_new, N, Np);
+  k_aos_to_cells<<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
+                                cudaStream_t s) {
+  if (N == 0) return cudaSuccess;
+  k_cells_to_aos<<<blocks(N, 256), 256, 0, s>>>(src, dst_aos, cell_new, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(const float* src, float* dst, const int* cell_new, int N, int Np,
+                              int rows, cudaStream_t s) {
+  if (N == 0) return cudaSuccess;
+  k_soa_to_aos<<<blocks(N, 256), 256, 0, s>>>(src, dst, cell_new, N, Np, rows);
   return cudaGetLastError();
 }
 

@@ -282,6 +282,17 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     hp.nd_ptr[d + 1] = int(hp.nd_cell.size());
   }
 
+  // node blocks: whole nodes, at most NODE_BLOCK_ENTRIES entries per block
+  hp.nb_ptr.assign(1, 0);
+  for (int d = 0; d < hp.Mc; ++d) {
+    const int cnt = hp.nd_ptr[d + 1] - hp.nd_ptr[d];
+    if (cnt > NODE_BLOCK_ENTRIES) return "a boundary node has more than 128 stencil cells";
+    if (hp.nd_ptr[d + 1] - hp.nd_ptr[hp.nb_ptr.back()] > NODE_BLOCK_ENTRIES ||
+        d - hp.nb_ptr.back() >= NODE_BLOCK_ENTRIES)
+      hp.nb_ptr.push_back(d);
+  }
+  if (hp.Mc > 0) hp.nb_ptr.push_back(hp.Mc);
+
   // ---- faces in device order (by lowest slot cell)
   {
     std::vector<std::pair<int64_t, int32_t>> fk(F);
@@ -353,16 +364,19 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
         break;
       }
     }
+  const HfRows HR{K, pr.flux_scheme, pr.variant};
+  hp.hrows = HR.rows();
+  auto hfi = [&](int i, int row) { return size_t(i >> 5) * size_t(hp.hrows) * 32 + size_t(row) * 32 + (i & 31); };
+  auto fbits = [](float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    return u;
+  };
   if (hp.fusable) {
-    hp.hf_code.assign(size_t(K) * hp.Np, 0);
-    hp.hf_nx.assign(size_t(K) * hp.Np, 0.0f);
-    hp.hf_ny.assign(size_t(K) * hp.Np, 0.0f);
-    hp.hf_L.assign(size_t(K) * hp.Np, 0.0f);
-    if (pr.flux_scheme == FVDBM_LAX_WENDROFF) {
-      hp.hf_r.assign(size_t(K) * hp.Np, 0.0f);
-      hp.hf_D2.assign(size_t(K) * hp.Np, 1.0f);
-    }
-    if (pr.variant == 1) hp.hf_scale.assign(size_t(K) * hp.Np, 1.0f);
+    hp.hf.assign(size_t(hp.Np / 32) * hp.hrows * 32, 0u);
+    if (pr.flux_scheme == FVDBM_LAX_WENDROFF)
+      for (int i = 0; i < hp.Np; ++i)
+        for (int k = 0; k < K; ++k) hp.hf[hfi(i, HR.d2(k))] = fbits(1.0f);
   }
   for (int i = 0; i < N; ++i) {
     const int c = hp.cell_old[i];
@@ -387,16 +401,16 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       } else {
         code |= hp.cell_new[oth] << HF_SHIFT;
       }
-      hp.hf_code[s] = code;
-      hp.hf_nx[s] = hp.fnx[j];
-      hp.hf_ny[s] = hp.fny[j];
+      hp.hf[hfi(i, HR.code(k))] = uint32_t(code);
+      hp.hf[hfi(i, HR.nx(k))] = fbits(hp.fnx[j]);
+      hp.hf[hfi(i, HR.ny(k))] = fbits(hp.fny[j]);
       // ((phi*v)*L)*sigma == (phi*v)*(L*sigma) exactly for sigma in {-1,0,1}
-      hp.hf_L[s] = hp.fL[j] * float(sg);
+      hp.hf[hfi(i, HR.ls(k))] = fbits(hp.fL[j] * float(sg));
       if (pr.flux_scheme == FVDBM_LAX_WENDROFF) {
-        hp.hf_r[s] = hp.fr[j];
-        hp.hf_D2[s] = hp.fD2[j];
+        hp.hf[hfi(i, HR.r(k))] = fbits(hp.fr[j]);
+        hp.hf[hfi(i, HR.d2(k))] = fbits(hp.fD2[j]);
       }
-      if (pr.variant == 1) hp.hf_scale[s] = hp.fscale[j];
+      if (pr.variant == 1) hp.hf[hfi(i, HR.sc(k))] = fbits(hp.fscale[j]);
     }
   }
   // ---- tile tables: per tile the nodes its ghost faces need (plus owner-only
@@ -433,7 +447,7 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       const int i1 = std::min(N, (t + 1) * TILE);
       for (int i = t * TILE; i < i1; ++i)
         for (int k = 0; k < K; ++k) {
-          const int32_t code = hp.hf_code[size_t(k) * hp.Np + i];
+          const int32_t code = int32_t(hp.hf[hfi(i, HR.code(k))]);
           if (!(code & HF_GHOST)) continue;
           const int g = code >> HF_SHIFT;
           add(hp.gh_a[g]);

@@ -2,11 +2,12 @@
 //
 // The cells are cut into tiles of TILE consecutive cells (device order, which
 // is Morton order when centroids are known).  Each CTA walks its tiles; for
-// each tile one thread issues bulk async copies (cp.async.bulk, completion
-// counted on an mbarrier) of the tile's 9 pdf rows and its per-face-slot rows
-// (neighbour code, normal, signed length, and the Lax-Wendroff / stencil
-// scale rows when used) into shared memory, double-buffered so that the next
-// tile streams in while this one computes.  Then:
+// each tile one thread issues two bulk async copies (cp.async.bulk,
+// completion counted on an mbarrier): the tile's pdfs and its per-face-slot
+// words (neighbour code, normal, signed length, and the Lax-Wendroff /
+// stencil scale rows when used), both contiguous in the AoSoA layout, into
+// shared memory, double-buffered so that the next tile streams in while this
+// one computes.  Then:
 //   phase A  the boundary nodes that the tile's ghost faces need
 //            (Nodes.calc_pdfs, src/containers.py:339-404): one thread per
 //            node-stencil entry evaluates that cell's macros, equilibrium and
@@ -70,53 +71,29 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 template <int SCHEME, int VARIANT>
 struct TileRows {
   static constexpr int K = 3;
-  static constexpr int F = 0;               // 9 pdf rows
-  static constexpr int CODE = 9;            // K rows each
-  static constexpr int NX = CODE + K;
-  static constexpr int NY = NX + K;
-  static constexpr int LS = NY + K;
-  static constexpr int R = LS + K;          // Lax-Wendroff d0/(d0+d1)
-  static constexpr int D2 = R + (SCHEME == 1 ? K : 0);
-  static constexpr int SC = D2 + (SCHEME == 1 ? K : 0);
-  static constexpr int ROWS = SC + (VARIANT == 1 ? K : 0);
+  static constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * K;
+  static constexpr int FWORDS = TILE * Q;      // the tile's pdfs, AoSoA
+  static constexpr int HWORDS = TILE * HROWS;  // the tile's face slots, AoSoA
+  static constexpr int WORDS = FWORDS + HWORDS;
 };
 
-template <int SCHEME, int VARIANT>
-__device__ __forceinline__ const void* row_src(const DevPlan& p, const float* fin, int r) {
-  using RW = TileRows<SCHEME, VARIANT>;
-  const size_t Np = p.Np;
-  if (r < RW::CODE) return fin + size_t(r) * Np;
-  if (r < RW::NX) return p.hf_code + size_t(r - RW::CODE) * Np;
-  if (r < RW::NY) return p.hf_nx + size_t(r - RW::NX) * Np;
-  if (r < RW::LS) return p.hf_ny + size_t(r - RW::NY) * Np;
-  if (r < RW::R) return p.hf_L + size_t(r - RW::LS) * Np;
-  if (SCHEME == 1 && r < RW::D2) return p.hf_r + size_t(r - RW::R) * Np;
-  if (SCHEME == 1 && r < RW::SC) return p.hf_D2 + size_t(r - RW::D2) * Np;
-  return p.hf_scale + size_t(r - RW::SC) * Np;
-}
-
-// Called by all 32 lanes of warp 0: lane 0 posts the byte count, then the
-// lanes issue one row copy each (ROWS <= 32).
+// A tile is TILE/32 consecutive AoSoA blocks, so its pdfs and its face slots
+// are two contiguous ranges: one bulk copy each (lane 0 of warp 0).
 template <int SCHEME, int VARIANT>
 __device__ __forceinline__ void issue_tile(const DevPlan& p, const float* fin, int tile, float* stage,
                                            uint32_t bar, int lane) {
   using RW = TileRows<SCHEME, VARIANT>;
-  static_assert(RW::ROWS <= 32, "one row per lane");
-  constexpr uint32_t row_bytes = TILE * sizeof(float);
-  if (lane == 0) mbar_expect_tx(bar, RW::ROWS * row_bytes);
-  __syncwarp();
-  if (lane < RW::ROWS) {
-    const float* src =
-        static_cast<const float*>(row_src<SCHEME, VARIANT>(p, fin, lane)) + size_t(tile) * TILE;
-    bulk_g2s(smem_u32(stage + lane * TILE), src, row_bytes, bar);
-  }
+  if (lane != 0) return;
+  mbar_expect_tx(bar, RW::WORDS * 4);
+  bulk_g2s(smem_u32(stage), fin + size_t(tile) * RW::FWORDS, RW::FWORDS * 4, bar);
+  bulk_g2s(smem_u32(stage + RW::FWORDS), p.hf + size_t(tile) * RW::HWORDS, RW::HWORDS * 4, bar);
 }
 
 }  // namespace
 
 template <int SCHEME, int VARIANT>
 constexpr size_t tile_smem_bytes() {
-  return (size_t(2) * TileRows<SCHEME, VARIANT>::ROWS * TILE + size_t(Q) * TILE_MAX_NODES +
+  return (size_t(2) * TileRows<SCHEME, VARIANT>::WORDS + size_t(Q) * TILE_MAX_NODES +
           size_t(12) * TILE_MAX_ENTRIES) * sizeof(float) + 2 * sizeof(uint64_t);
 }
 
@@ -127,13 +104,12 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
   constexpr int K = RW::K;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float* stage0 = reinterpret_cast<float*>(smem_raw);
-  float* npdf = stage0 + 2 * RW::ROWS * TILE;      // [9][TILE_MAX_NODES]
+  float* npdf = stage0 + 2 * RW::WORDS;            // [9][TILE_MAX_NODES]
   float* prod = npdf + Q * TILE_MAX_NODES;          // [12][TILE_MAX_ENTRIES]
   uint64_t* bars = reinterpret_cast<uint64_t*>(prod + 12 * TILE_MAX_ENTRIES);
   const int tid = threadIdx.x;
   const int first = blockIdx.x, stride = gridDim.x;
   if (first >= p.NT) return;
-  const size_t Np = p.Np;
   const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
 
   if (tid == 0) {
@@ -145,7 +121,7 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
   if (tid < 32) {
     issue_tile<SCHEME, VARIANT>(p, fin, first, stage0, bar0, tid);
     if (first + stride < p.NT)
-      issue_tile<SCHEME, VARIANT>(p, fin, first + stride, stage0 + RW::ROWS * TILE, bar1, tid);
+      issue_tile<SCHEME, VARIANT>(p, fin, first + stride, stage0 + RW::WORDS, bar1, tid);
   }
 
   int it = 0;
@@ -171,10 +147,11 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
       if (tn < p.NT) {
         if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
-        issue_tile<SCHEME, VARIANT>(p, fin, tn, stage0 + (s ^ 1) * RW::ROWS * TILE, s ? bar0 : bar1, tid);
+        issue_tile<SCHEME, VARIANT>(p, fin, tn, stage0 + (s ^ 1) * RW::WORDS, s ? bar0 : bar1, tid);
       }
     }
-    const float* S = stage0 + s * RW::ROWS * TILE;
+    const float* SF = stage0 + s * RW::WORDS;  // pdfs, AoSoA
+    const unsigned* SH = reinterpret_cast<const unsigned*>(SF + RW::FWORDS);  // face slots, AoSoA
     const int tile_start = t * TILE;
 
     // ---- phase A: boundary nodes needed by this tile
@@ -189,11 +166,11 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
         float fc[Q], eq[Q];
         const unsigned lc = unsigned(c - tile_start);
         if (lc < unsigned(TILE)) {
+          const float* b = SF + cell_base(int(lc), Q);
 #pragma unroll
-          for (int q = 0; q < Q; ++q) fc[q] = S[(RW::F + q) * TILE + lc];
+          for (int q = 0; q < Q; ++q) fc[q] = b[q * 32];
         } else {
-#pragma unroll
-          for (int q = 0; q < Q; ++q) fc[q] = __ldg(fin + q * Np + c);
+          load_cell(fin, c, fc);
         }
         float rho, ux, uy;
         macros(fc, rho, ux, uy);
@@ -237,8 +214,7 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
           if (__ldg(p.tn_npad + nb + tid) > 0) {
             // padded (-1, weight 0) entries gather the last cell: rho*0, u*0
             float fc[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) fc[q] = __ldg(fin + q * Np + p.last_cell);
+            load_cell(fin, p.last_cell, fc);
             float rho, ux, uy;
             macros(fc, rho, ux, uy);
             ar = cnt ? ar + rho * 0.0f : rho * 0.0f;
@@ -281,18 +257,23 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
     const int i = tile_start + tid;
     if (i < p.N) {
       float f[Q];
+      {
+        const float* b = SF + cell_base(tid, Q);
 #pragma unroll
-      for (int q = 0; q < Q; ++q) f[q] = S[(RW::F + q) * TILE + tid];
+        for (int q = 0; q < Q; ++q) f[q] = b[q * 32];
+      }
+      const unsigned* hb = SH + cell_base(tid, RW::HROWS);
+      const HfRows HR{K, SCHEME, VARIANT};
       float rho, ux, uy, eq[Q];
       macros(f, rho, ux, uy);
       feq9(rho, ux, uy, p, eq);
       float acc[Q];
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        const int code = __float_as_int(S[(RW::CODE + k) * TILE + tid]);
-        const float nx = S[(RW::NX + k) * TILE + tid];
-        const float ny = S[(RW::NY + k) * TILE + tid];
-        const float Ls = S[(RW::LS + k) * TILE + tid];
+        const int code = int(hb[HR.code(k) * 32]);
+        const float nx = __uint_as_float(hb[HR.nx(k) * 32]);
+        const float ny = __uint_as_float(hb[HR.ny(k) * 32]);
+        const float Ls = __uint_as_float(hb[HR.ls(k) * 32]);
         const int other = code >> HF_SHIFT;
         const bool slot1 = (code & HF_SLOT1) != 0;
         float o[Q];
@@ -317,19 +298,19 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
         } else {
           const unsigned lo = unsigned(other - tile_start);
           if (lo < unsigned(TILE)) {
+            const float* b = SF + cell_base(int(lo), Q);
 #pragma unroll
-            for (int q = 0; q < Q; ++q) o[q] = S[(RW::F + q) * TILE + lo];
+            for (int q = 0; q < Q; ++q) o[q] = b[q * 32];
           } else {
-#pragma unroll
-            for (int q = 0; q < Q; ++q) o[q] = __ldg(fin + q * Np + other);
+            load_cell(fin, other, o);
           }
         }
         float v[Q], w[Q];
         xi_dot_n(nx, ny, p.finite_n != 0, v);
         if (SCHEME == 1)
-          lw_interp(v, S[(RW::R + k) * TILE + tid], S[(RW::D2 + k) * TILE + tid], p.dt,
+          lw_interp(v, __uint_as_float(hb[HR.r(k) * 32]), __uint_as_float(hb[HR.d2(k) * 32]), p.dt,
                     p.finite_n != 0, w);
-        const float scale = (VARIANT == 1) ? S[(RW::SC + k) * TILE + tid] : 1.0f;
+        const float scale = (VARIANT == 1) ? __uint_as_float(hb[HR.sc(k) * 32]) : 1.0f;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
           float phi;
@@ -349,9 +330,9 @@ __global__ void __launch_bounds__(TILE, 2) k_tile(DevPlan p, const float* __rest
 #pragma unroll
         for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
       }
+      float* ob = fout + cell_base(i, Q);
 #pragma unroll
-      for (int q = 0; q < Q; ++q)
-        fout[q * Np + i] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+      for (int q = 0; q < Q; ++q) ob[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
     }
 
   }
