@@ -151,6 +151,9 @@ int upload_nodes(Handle* h) {
   return FVDBM_OK;
 }
 
+// Back-to-back steps use programmatic dependent launch between the node and
+// cell kernels (each waits for its predecessor before reading its output);
+// the first launch of a call follows whatever preceded it in the stream.
 int enqueue_steps(Handle* h, int n) {
   for (int s = 0; s < n; ++s) {
     const float* fin = h->f[h->cur];
@@ -159,9 +162,9 @@ int enqueue_steps(Handle* h, int n) {
       if (!h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
       CK(launch_tile(h->dp, fin, fout, h->stream));
     } else {
-      CK(launch_nodes(h->dp, fin, h->stream));
+      CK(launch_nodes(h->dp, fin, h->stream, /*pdl=*/s > 0));
       if (h->fused) {
-        CK(launch_fused(h->dp, fin, fout, h->stream));
+        CK(launch_fused(h->dp, fin, fout, h->stream, /*pdl=*/h->dp.NB > 0 || s > 0));
       } else {
         CK(launch_face_flux(h->dp, fin, h->flux, h->stream));
         CK(launch_gather(h->dp, fin, h->flux, fout, h->stream));
@@ -342,8 +345,8 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   UP(nd_cell, hp.nd_cell);
   UP(nd_w, hp.nd_w);
   UP(nd_sumw, hp.nd_sumw);
-  UP(nb_ptr, hp.nb_ptr);
-  p.NB = hp.nb_ptr.empty() ? 0 : int(hp.nb_ptr.size()) - 1;
+  UP(nb_meta, hp.nb_meta);
+  p.NB = int(hp.nb_meta.size() / 4);
   UP(inv_area, hp.inv_area);
   p.NT = hp.NT;
   if (h->tile) {

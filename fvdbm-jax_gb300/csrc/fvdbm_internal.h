@@ -85,8 +85,8 @@ struct HostPlan {
   std::vector<int32_t> gh_a, gh_b;
   std::vector<float> gh_r;
   // node blocks of the node kernel: contiguous computed nodes with at most
-  // NODE_BLOCK_ENTRIES stencil entries each
-  std::vector<int32_t> nb_ptr;
+  // NODE_BLOCK_ENTRIES stencil entries each; nb_meta = 4 ints per block
+  std::vector<int32_t> nb_ptr, nb_meta;
 
   // nodes on the device: computed (type 1/2) first, then frozen ghost ends
   int M = 0, Mc = 0, Mp = 0;
@@ -162,7 +162,7 @@ struct DevPlan {
   const unsigned* nd_cell;
   const float* nd_w;
   const float* nd_sumw;
-  const int* nb_ptr;  // node blocks
+  const int* nb_meta;  // node blocks: {first node, end node, first entry, end entry}
   int NB;
   float* node_pdf;  // [9][Mp]
   float* node_rho;  // [Mp]
@@ -189,8 +189,10 @@ struct DevPlan {
 constexpr int STATUS_WAIT_TIMEOUT = 1;
 
 // kernel launchers (kernels.cu)
-cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s);
-cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
+// pdl: launch with programmatic dependent launch after a step kernel
+cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s, bool pdl = false);
+cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
+                         bool pdl = false);
 cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);
 // Persistent tile kernel (tile.cu): one launch per step.  prepare_tile sets
 // the kernel's shared-memory attribute and grid size; call it outside any

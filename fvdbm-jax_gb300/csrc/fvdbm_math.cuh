@@ -23,6 +23,12 @@ static __constant__ float c_W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (f
 
 __device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
 
+// Programmatic dependent launch: wait until the previous kernel in the
+// stream has completed and its writes are visible (a no-op when the kernel
+// was launched without the attribute); let the next kernel start launching.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // Cell arrays are AoSoA: blocks of 32 cells, [block][row][32].  A cell's
 // row r sits at cell_base(i) + r*32, a constant offset from one base.
 __device__ __forceinline__ size_t cell_base(int i, int rows) {

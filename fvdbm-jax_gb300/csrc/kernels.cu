@@ -5,6 +5,8 @@
 // Layout: cell pdfs are AoSoA [Np/32][9][32] float32 in device (renumbered)
 // cell order; the fused kernel's per-cell face slots are AoSoA
 // [Np/32][hrows][32]; node state is SoA [9][Mp].
+#include <utility>
+
 #include "fvdbm_math.cuh"
 
 namespace fvdbm {
@@ -22,14 +24,39 @@ namespace fvdbm {
 __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const float* __restrict__ f) {
   __shared__ float prod[12][NODE_BLOCK_ENTRIES];
   __shared__ float fold[12][NODE_BLOCK_ENTRIES];
+  __shared__ int nptr[NODE_BLOCK_ENTRIES + 1];
+  __shared__ int npad[NODE_BLOCK_ENTRIES];
+  __shared__ float nsw[NODE_BLOCK_ENTRIES];
+  __shared__ float nset[3][NODE_BLOCK_ENTRIES];  // type: +1 velocity / -1 density, set vx, vy | rho
   __shared__ float lastm[3];
-  const int n0 = __ldg(p.nb_ptr + blockIdx.x), n1 = __ldg(p.nb_ptr + blockIdx.x + 1);
-  const int nn = n1 - n0;
-  const int e0 = __ldg(p.nd_ptr + n0), ne = __ldg(p.nd_ptr + n1) - e0;
+  grid_dep_launch();
+  const int4 meta = __ldg(reinterpret_cast<const int4*>(p.nb_meta) + blockIdx.x);  // n0, n1, e0, e1
+  const int n0 = meta.x, nn = meta.y - meta.x, e0 = meta.z, ne = meta.w - meta.z;
   const int tid = threadIdx.x;
+  // per-node metadata, once, while the entries load
+  if (tid < nn) {
+    const int m = n0 + tid;
+    nptr[tid] = __ldg(p.nd_ptr + m) - e0;
+    if (tid == nn - 1) nptr[nn] = ne;
+    npad[tid] = __ldg(p.nd_npad + m);
+    nsw[tid] = __ldg(p.nd_sumw + m);
+    const int type = __ldg(p.nd_type + m);
+    nset[0][tid] = type == 1 ? 1.0f : -1.0f;
+    if (type == 1) {
+      nset[1][tid] = p.node_vel[m];
+      nset[2][tid] = p.node_vel[p.Mp + m];
+    } else {
+      nset[1][tid] = p.node_rho[m];
+    }
+  }
+  unsigned code = 0;
+  float w = 0.0f;
   if (tid < ne) {
-    const unsigned code = __ldg(p.nd_cell + e0 + tid);
-    const float w = __ldg(p.nd_w + e0 + tid);
+    code = __ldg(p.nd_cell + e0 + tid);
+    w = __ldg(p.nd_w + e0 + tid);
+  }
+  grid_dep_wait();  // f comes from the previous cell kernel
+  if (tid < ne) {
     float fc[Q], eq[Q];
     load_cell(f, int(code & ~ND_NEQ_ZERO), fc);
     float rho, ux, uy;
@@ -54,12 +81,11 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
   }
   __syncthreads();
   for (int idx = tid; idx < nn * 12; idx += NODE_BLOCK_ENTRIES) {
-    const int j = idx / 12, r = idx % 12;
-    const int m = n0 + j;
-    const int b = __ldg(p.nd_ptr + m) - e0, cnt = __ldg(p.nd_ptr + m + 1) - e0 - b;
+    const int j = idx / 12, r = idx - 12 * (idx / 12);
+    const int b = nptr[j], cnt = nptr[j + 1] - b;
     float acc = 0.0f;
     for (int k = 0; k < cnt; ++k) acc = k ? acc + prod[r][b + k] : prod[r][b];
-    if (r < 3 && __ldg(p.nd_npad + m) > 0) {
+    if (r < 3 && npad[j] > 0) {
       const float z = lastm[r] * 0.0f;
       acc = cnt ? acc + z : z;
     }
@@ -67,23 +93,23 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
   }
   __syncthreads();
   for (int idx = tid; idx < nn * Q; idx += NODE_BLOCK_ENTRIES) {
-    const int j = idx / Q, q = idx % Q;
+    const int j = idx / Q, q = idx - Q * (idx / Q);
     const int m = n0 + j;
-    const float sw = __ldg(p.nd_sumw + m);
-    const int type = __ldg(p.nd_type + m);
+    const float sw = nsw[j];
+    const bool vel_node = nset[0][j] > 0.0f;
     float rho_p, ux_p, uy_p;
-    if (type == 1) {
+    if (vel_node) {
       rho_p = fold[0][j] / sw;
-      ux_p = p.node_vel[m];
-      uy_p = p.node_vel[p.Mp + m];
+      ux_p = nset[1][j];
+      uy_p = nset[2][j];
     } else {
-      rho_p = p.node_rho[m];
+      rho_p = nset[1][j];
       ux_p = fold[1][j] / sw;
       uy_p = fold[2][j] / sw;
     }
     p.node_pdf[size_t(q) * p.Mp + m] = feq_one(rho_p, ux_p, uy_p, q, p) + fold[3 + q][j] / sw;
     if (q == 0) {
-      if (type == 1) {
+      if (vel_node) {
         p.node_rho[m] = rho_p;
       } else {
         p.node_vel[m] = ux_p;
@@ -100,13 +126,9 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
 // and the BGK/explicit-Euler update (src/containers.py:107-121).
 template <int SCHEME, int VARIANT, bool FIRST>
 __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin,
-                                           const unsigned* __restrict__ hb, int k, const float f[Q],
-                                           float acc[Q]) {
+                                           const unsigned* __restrict__ hb, int k, int code, float nx,
+                                           float ny, float Ls, const float f[Q], float acc[Q]) {
   const HfRows HR{3, SCHEME, VARIANT};
-  const int code = int(__ldg(hb + HR.code(k) * 32));
-  const float nx = __uint_as_float(__ldg(hb + HR.nx(k) * 32));
-  const float ny = __uint_as_float(__ldg(hb + HR.ny(k) * 32));
-  const float Ls = __uint_as_float(__ldg(hb + HR.ls(k) * 32));  // L * sigma
   const int other = code >> HF_SHIFT;
   const bool slot1 = (code & HF_SLOT1) != 0;
   float o[Q];
@@ -155,27 +177,35 @@ template <int SCHEME, int VARIANT, bool FV>
 __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restrict__ fin,
                                                float* __restrict__ fout, int prefetch_blocks) {
   constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+  grid_dep_launch();
   // the block about one wave ahead streams into L2 while this one computes
-  if (threadIdx.x == 0 && prefetch_blocks > 0) {
-    const int ahead = blockIdx.x + prefetch_blocks;
-    if (ahead < int(gridDim.x)) {
-      const size_t c0 = size_t(ahead) * 256;
-      prefetch_l2(fin + c0 * Q, 256 * Q * sizeof(float));
-      prefetch_l2(p.hf + c0 * HROWS, 256 * HROWS * sizeof(unsigned));
-    }
-  }
+  const int ahead = blockIdx.x + prefetch_blocks;
+  const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead < int(gridDim.x);
+  if (do_prefetch) prefetch_l2(p.hf + size_t(ahead) * 256 * HROWS, 256 * HROWS * sizeof(unsigned));
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const HfRows HR{3, SCHEME, VARIANT};
+  const unsigned* hb = p.hf + cell_base(i < p.N ? i : 0, HROWS);
+  int code[3];
+  float nx[3], ny[3], Ls[3];  // Ls = L * sigma
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    code[k] = int(__ldg(hb + HR.code(k) * 32));
+    nx[k] = __uint_as_float(__ldg(hb + HR.nx(k) * 32));
+    ny[k] = __uint_as_float(__ldg(hb + HR.ny(k) * 32));
+    Ls[k] = __uint_as_float(__ldg(hb + HR.ls(k) * 32));
+  }
+  grid_dep_wait();  // fin and the node pdfs come from the previous kernels
+  if (do_prefetch) prefetch_l2(fin + size_t(ahead) * 256 * Q, 256 * Q * sizeof(float));
   if (i >= p.N) return;
   float f[Q];
   load_cell(fin, i, f);
   float rho, ux, uy, eq[Q];
   macros(f, rho, ux, uy);
   feq9(rho, ux, uy, p, eq);
-  const unsigned* hb = p.hf + cell_base(i, HROWS);
   float acc[Q];
-  fused_face<SCHEME, VARIANT, true>(p, fin, hb, 0, f, acc);
-  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 1, f, acc);
-  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 2, f, acc);
+  fused_face<SCHEME, VARIANT, true>(p, fin, hb, 0, code[0], nx[0], ny[0], Ls[0], f, acc);
+  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 1, code[1], nx[1], ny[1], Ls[1], f, acc);
+  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 2, code[2], nx[2], ny[2], Ls[2], f, acc);
   if (FV) {
     const float ia = __ldg(p.inv_area + i);
 #pragma unroll
@@ -356,10 +386,28 @@ __global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, unsigned 
 // ---------------------------------------------------------------------------
 static inline int blocks(long long n, int t) { return int((n + t - 1) / t); }
 
-cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s) {
+// Launch with programmatic stream serialization when pdl is set: the kernel
+// may start while its predecessor drains; it synchronises with
+// griddepcontrol.wait before touching the predecessor's output.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_ex(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                             bool pdl, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
+cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s, bool pdl) {
   if (p.NB == 0) return cudaSuccess;
-  k_nodes<<<p.NB, NODE_BLOCK_ENTRIES, 0, s>>>(p, f);
-  return cudaGetLastError();
+  return launch_ex(k_nodes, p.NB, NODE_BLOCK_ENTRIES, 0, s, pdl, p, f);
 }
 
 static int fused_prefetch_blocks() {
@@ -374,22 +422,22 @@ static int fused_prefetch_blocks() {
 }
 
 template <int S, int V>
-static void fused_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
+static cudaError_t fused_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
+                                  bool pdl) {
   const int g = blocks(p.N, 256);
   const int pf = fused_prefetch_blocks();
-  if (p.fv) k_fused<S, V, true><<<g, 256, 0, s>>>(p, fin, fout, pf);
-  else k_fused<S, V, false><<<g, 256, 0, s>>>(p, fin, fout, pf);
+  if (p.fv) return launch_ex(k_fused<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, pf);
+  return launch_ex(k_fused<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, pf);
 }
 
-cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
+cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl) {
   if (p.N == 0) return cudaSuccess;
   if (p.K != 3) return cudaErrorInvalidValue;
-  if (p.scheme == 0 && p.variant == 0) fused_dispatch<0, 0>(p, fin, fout, s);
-  else if (p.scheme == 1 && p.variant == 0) fused_dispatch<1, 0>(p, fin, fout, s);
-  else if (p.scheme == 0 && p.variant == 1) fused_dispatch<0, 1>(p, fin, fout, s);
-  else if (p.scheme == 1 && p.variant == 1) fused_dispatch<1, 1>(p, fin, fout, s);
-  else return cudaErrorInvalidValue;
-  return cudaGetLastError();
+  if (p.scheme == 0 && p.variant == 0) return fused_dispatch<0, 0>(p, fin, fout, s, pdl);
+  if (p.scheme == 1 && p.variant == 0) return fused_dispatch<1, 0>(p, fin, fout, s, pdl);
+  if (p.scheme == 0 && p.variant == 1) return fused_dispatch<0, 1>(p, fin, fout, s, pdl);
+  if (p.scheme == 1 && p.variant == 1) return fused_dispatch<1, 1>(p, fin, fout, s, pdl);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s) {

@@ -292,6 +292,13 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       hp.nb_ptr.push_back(d);
   }
   if (hp.Mc > 0) hp.nb_ptr.push_back(hp.Mc);
+  hp.nb_meta.clear();
+  for (size_t b = 0; b + 1 < hp.nb_ptr.size(); ++b) {
+    hp.nb_meta.push_back(hp.nb_ptr[b]);
+    hp.nb_meta.push_back(hp.nb_ptr[b + 1]);
+    hp.nb_meta.push_back(hp.nd_ptr[hp.nb_ptr[b]]);
+    hp.nb_meta.push_back(hp.nd_ptr[hp.nb_ptr[b + 1]]);
+  }
 
   // ---- faces in device order (by lowest slot cell)
   {
