@@ -36,6 +36,7 @@ struct Handle {
   long long steps_done = 0;
   bool fused = false;
   bool tile = false;
+  bool one = false;  // node and cell blocks in one launch
   int* status = nullptr;
   std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -158,7 +159,9 @@ int enqueue_steps(Handle* h, int n) {
   for (int s = 0; s < n; ++s) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
-    if (h->tile) {
+    if (h->one) {
+      CK(launch_step(h->dp, fin, fout, h->stream, /*pdl=*/s > 0));
+    } else if (h->tile) {
       if (!h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
       CK(launch_tile(h->dp, fin, fout, h->stream));
     } else {
@@ -286,6 +289,13 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
     return create_fail(h, FVDBM_EINVAL);
   }
   h->tile = tile_possible && want_tile;
+  const bool one_possible = hp.fusable && hp.K == 3 && hp.N > 0;
+  if (params->kernel == FVDBM_KERNEL_ONE && !one_possible) {
+    h->err = "the single-launch step needs triangles (3 face slots per cell), every cell face slot "
+             "naming a face of that cell, and no per-q flux scale";
+    return create_fail(h, FVDBM_EINVAL);
+  }
+  h->one = one_possible && (params->kernel == FVDBM_KERNEL_ONE || params->kernel == FVDBM_KERNEL_AUTO);
   h->dp.tile_nodes = (params->kernel == FVDBM_KERNEL_TILE) ? 1 : 0;
   p.N = hp.N;
   p.Np = hp.Np;
@@ -363,9 +373,11 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
     UP(tgh_a, hp.tgh_a);
     UP(tgh_b, hp.tgh_b);
   }
-  if ((rc = dalloc<int>(h, &h->status, 1)) != FVDBM_OK) return create_fail(h, rc);
-  CR(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+  if ((rc = dalloc<int>(h, &h->status, 4)) != FVDBM_OK) return create_fail(h, rc);
+  CR(cudaMemsetAsync(h->status, 0, 4 * sizeof(int), h->stream));
   p.status = h->status;
+  p.step_ctr = h->status + 1;
+  if (h->fused) UP(cblk_ghost, hp.cblk_ghost);
   if (h->tile) CR(prepare_tile(p));
   {
     float* d = nullptr;
@@ -479,9 +491,11 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
   if (phase == 1) {
-    if (!h->tile || !h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
+    if (!h->one && (!h->tile || !h->dp.tile_nodes)) CK(launch_nodes(h->dp, fin, h->stream));
   } else if (phase == 2) {
-    if (h->tile) {
+    if (h->one) {
+      CK(launch_step(h->dp, fin, fout, h->stream, false));
+    } else if (h->tile) {
       CK(launch_tile(h->dp, fin, fout, h->stream));
     } else if (h->fused) {
       CK(launch_fused(h->dp, fin, fout, h->stream));
@@ -608,10 +622,11 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
-                          : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
-  const int node_launch = (hp.Mc > 0 && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
-  info->launches_per_step = node_launch + (h->tile ? 1 : (h->fused ? 1 : 2));
+  info->kernel = h->one ? FVDBM_KERNEL_ONE
+                         : h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
+                                   : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
+  const int node_launch = (hp.Mc > 0 && !h->one && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
+  info->launches_per_step = node_launch + (h->one || h->tile ? 1 : (h->fused ? 1 : 2));
   info->padded_cells = hp.Np;
   info->ctas_per_sm = h->tile ? tile_ctas_per_sm(h->dp) : 0;
   info->const_division = (h->dp.d_c2.ok && h->dp.d_c4x2.ok && h->dp.d_c2x2.ok) ? 1 : 0;

@@ -28,7 +28,7 @@ constexpr int TILE = 256;
 constexpr int TILE_MAX_NODES = 128;    // nodes evaluated per tile
 constexpr int TILE_MAX_ENTRIES = 256;  // node-stencil cells per tile
 constexpr int TN_OWNER = 1 << 4;       // tn_kind flag: this tile writes the node state
-constexpr int NODE_BLOCK_ENTRIES = 128; // node kernel: entries (= threads) per block
+constexpr int NODE_BLOCK_ENTRIES = 256; // node blocks: entries (= threads) per block
 
 // rows of the half-face array for K face slots
 struct HfRows {
@@ -87,6 +87,7 @@ struct HostPlan {
   // node blocks of the node kernel: contiguous computed nodes with at most
   // NODE_BLOCK_ENTRIES stencil entries each; nb_meta = 4 ints per block
   std::vector<int32_t> nb_ptr, nb_meta;
+  std::vector<uint8_t> cblk_ghost;  // per 256-cell block: any ghost face
 
   // nodes on the device: computed (type 1/2) first, then frozen ghost ends
   int M = 0, Mc = 0, Mp = 0;
@@ -184,6 +185,8 @@ struct DevPlan {
   const int* tgh_a;
   const int* tgh_b;
   int* status;  // device status word (0 ok); set when a bounded wait gives up
+  int* step_ctr;  // single-launch step: ticket, node blocks published, blocks finished
+  const unsigned char* cblk_ghost;  // per 256-cell block: has a ghost face
 };
 
 constexpr int STATUS_WAIT_TIMEOUT = 1;
@@ -193,6 +196,8 @@ constexpr int STATUS_WAIT_TIMEOUT = 1;
 cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s, bool pdl = false);
 cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
                          bool pdl = false);
+// the whole step in one launch (node blocks then cell blocks, see kernels.cu)
+cudaError_t launch_step(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl);
 cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);
 // Persistent tile kernel (tile.cu): one launch per step.  prepare_tile sets
 // the kernel's shared-memory attribute and grid size; call it outside any

@@ -15,38 +15,33 @@ namespace fvdbm {
 // Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  A block holds
 // whole nodes with at most NODE_BLOCK_ENTRIES stencil entries:
 //   1. one thread per entry: that cell's macros, feq and the IDW products
-//      rho*w, u*w, (f - feq)*w (utils/utils.py:34-60);
-//   2. one thread per (node, component): the ordered fold over the node's
-//      entries (the reference's sum order);
-//   3. one thread per (node, q): velocity nodes (type 1) take rho =
-//      IDW(cell rho), density nodes (type 2) take u = IDW(cell u);
-//      pdf_q = feq_q(rho, u) + IDW(f - feq)_q.
-__global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const float* __restrict__ f) {
-  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
-  __shared__ float fold[12][NODE_BLOCK_ENTRIES];
-  __shared__ int nptr[NODE_BLOCK_ENTRIES + 1];
-  __shared__ int npad[NODE_BLOCK_ENTRIES];
-  __shared__ float nsw[NODE_BLOCK_ENTRIES];
-  __shared__ float nset[3][NODE_BLOCK_ENTRIES];  // type: +1 velocity / -1 density, set vx, vy | rho
-  __shared__ float lastm[3];
-  grid_dep_launch();
-  const int4 meta = __ldg(reinterpret_cast<const int4*>(p.nb_meta) + blockIdx.x);  // n0, n1, e0, e1
+//      rho*w, u*w, (f - feq)*w (utils/utils.py:34-60) into shared memory;
+//   2. one thread per node: the ordered folds over the node's entries (the
+//      reference's sum order), then velocity nodes (type 1) take rho =
+//      IDW(cell rho), density nodes (type 2) take u = IDW(cell u), and
+//      pdf = feq(rho, u) + IDW(f - feq).
+// WAIT: call grid_dep_wait() before reading f (false when the caller did).
+template <bool WAIT>
+__device__ __forceinline__ void node_block(const DevPlan& p, const float* __restrict__ f, int blk,
+                                           float (*prod)[NODE_BLOCK_ENTRIES], float* lastm) {
+  const int4 meta = __ldg(reinterpret_cast<const int4*>(p.nb_meta) + blk);  // n0, n1, e0, e1
   const int n0 = meta.x, nn = meta.y - meta.x, e0 = meta.z, ne = meta.w - meta.z;
   const int tid = threadIdx.x;
-  // per-node metadata, once, while the entries load
+  // static tables first (they do not depend on the previous kernel)
+  int b = 0, cnt = 0, npad = 0, type = 0;
+  float sw = 0.0f, set0 = 0.0f, set1 = 0.0f;
   if (tid < nn) {
     const int m = n0 + tid;
-    nptr[tid] = __ldg(p.nd_ptr + m) - e0;
-    if (tid == nn - 1) nptr[nn] = ne;
-    npad[tid] = __ldg(p.nd_npad + m);
-    nsw[tid] = __ldg(p.nd_sumw + m);
-    const int type = __ldg(p.nd_type + m);
-    nset[0][tid] = type == 1 ? 1.0f : -1.0f;
+    b = __ldg(p.nd_ptr + m) - e0;
+    cnt = __ldg(p.nd_ptr + m + 1) - e0 - b;
+    npad = __ldg(p.nd_npad + m);
+    sw = __ldg(p.nd_sumw + m);
+    type = __ldg(p.nd_type + m);
     if (type == 1) {
-      nset[1][tid] = p.node_vel[m];
-      nset[2][tid] = p.node_vel[p.Mp + m];
+      set0 = p.node_vel[m];
+      set1 = p.node_vel[p.Mp + m];
     } else {
-      nset[1][tid] = p.node_rho[m];
+      set0 = p.node_rho[m];
     }
   }
   unsigned code = 0;
@@ -55,7 +50,7 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
     code = __ldg(p.nd_cell + e0 + tid);
     w = __ldg(p.nd_w + e0 + tid);
   }
-  grid_dep_wait();  // f comes from the previous cell kernel
+  if (WAIT) grid_dep_wait();  // f comes from the previous cell kernel
   if (tid < ne) {
     float fc[Q], eq[Q];
     load_cell(f, int(code & ~ND_NEQ_ZERO), fc);
@@ -80,43 +75,46 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
     lastm[2] = uy;
   }
   __syncthreads();
-  for (int idx = tid; idx < nn * 12; idx += NODE_BLOCK_ENTRIES) {
-    const int j = idx / 12, r = idx - 12 * (idx / 12);
-    const int b = nptr[j], cnt = nptr[j + 1] - b;
-    float acc = 0.0f;
-    for (int k = 0; k < cnt; ++k) acc = k ? acc + prod[r][b + k] : prod[r][b];
-    if (r < 3 && npad[j] > 0) {
+  if (tid >= nn) return;  // (callers do not synchronise after this)
+  float acc[12];
+#pragma unroll
+  for (int r = 0; r < 12; ++r) acc[r] = 0.0f;
+  for (int k = 0; k < cnt; ++k) {
+#pragma unroll
+    for (int r = 0; r < 12; ++r) acc[r] = k ? acc[r] + prod[r][b + k] : prod[r][b + k];
+  }
+  if (npad > 0) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
       const float z = lastm[r] * 0.0f;
-      acc = cnt ? acc + z : z;
-    }
-    fold[r][j] = acc;
-  }
-  __syncthreads();
-  for (int idx = tid; idx < nn * Q; idx += NODE_BLOCK_ENTRIES) {
-    const int j = idx / Q, q = idx - Q * (idx / Q);
-    const int m = n0 + j;
-    const float sw = nsw[j];
-    const bool vel_node = nset[0][j] > 0.0f;
-    float rho_p, ux_p, uy_p;
-    if (vel_node) {
-      rho_p = fold[0][j] / sw;
-      ux_p = nset[1][j];
-      uy_p = nset[2][j];
-    } else {
-      rho_p = nset[1][j];
-      ux_p = fold[1][j] / sw;
-      uy_p = fold[2][j] / sw;
-    }
-    p.node_pdf[size_t(q) * p.Mp + m] = feq_one(rho_p, ux_p, uy_p, q, p) + fold[3 + q][j] / sw;
-    if (q == 0) {
-      if (vel_node) {
-        p.node_rho[m] = rho_p;
-      } else {
-        p.node_vel[m] = ux_p;
-        p.node_vel[p.Mp + m] = uy_p;
-      }
+      acc[r] = cnt ? acc[r] + z : z;
     }
   }
+  const int m = n0 + tid;
+  float rho_p, ux_p, uy_p;
+  if (type == 1) {
+    rho_p = acc[0] / sw;
+    ux_p = set0;
+    uy_p = set1;
+    p.node_rho[m] = rho_p;
+  } else {
+    rho_p = set0;
+    ux_p = acc[1] / sw;
+    uy_p = acc[2] / sw;
+    p.node_vel[m] = ux_p;
+    p.node_vel[p.Mp + m] = uy_p;
+  }
+  float eqn[Q];
+  feq9(rho_p, ux_p, uy_p, p, eqn);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) p.node_pdf[size_t(q) * p.Mp + m] = eqn[q] + acc[3 + q] / sw;
+}
+
+__global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const float* __restrict__ f) {
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  grid_dep_launch();
+  node_block<true>(p, f, blockIdx.x, prod, lastm);
 }
 
 // ---------------------------------------------------------------------------
@@ -124,7 +122,7 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
 // (recomputed from the canonical slot-0/slot-1 pair, so both neighbours get
 // bit-identical fluxes without a flux array or atomics), the signed flux sum
 // and the BGK/explicit-Euler update (src/containers.py:107-121).
-template <int SCHEME, int VARIANT, bool FIRST>
+template <int SCHEME, int VARIANT, bool FIRST, bool GHOST_CG>
 __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin,
                                            const unsigned* __restrict__ hb, int k, int code, float nx,
                                            float ny, float Ls, const float f[Q], float acc[Q]) {
@@ -139,8 +137,9 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
     const float rg = __ldg(p.gh_r + other);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      const float mq = (__ldg(p.node_pdf + size_t(q) * p.Mp + a) +
-                        __ldg(p.node_pdf + size_t(q) * p.Mp + b)) / 2.0f;
+      const float* pa = p.node_pdf + size_t(q) * p.Mp + a;
+      const float* pb = p.node_pdf + size_t(q) * p.Mp + b;
+      const float mq = (GHOST_CG ? (__ldcg(pa) + __ldcg(pb)) : (__ldg(pa) + __ldg(pb))) / 2.0f;
       o[q] = mq + (mq - f[q]) * rg;
     }
   } else {
@@ -173,6 +172,47 @@ __device__ __forceinline__ void prefetch_l2(const void* ptr, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
 }
 
+// One cell of the fused update.  GHOST_CG: read node pdfs through L2 (they
+// were written earlier in the same launch).
+template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG>
+__device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __restrict__ fin,
+                                           float* __restrict__ fout, int i, const int code[3],
+                                           const float nx[3], const float ny[3], const float Ls[3],
+                                           const unsigned* __restrict__ hb) {
+  float f[Q];
+  load_cell(fin, i, f);
+  float rho, ux, uy, eq[Q];
+  macros(f, rho, ux, uy);
+  feq9(rho, ux, uy, p, eq);
+  float acc[Q];
+  fused_face<SCHEME, VARIANT, true, GHOST_CG>(p, fin, hb, 0, code[0], nx[0], ny[0], Ls[0], f, acc);
+  fused_face<SCHEME, VARIANT, false, GHOST_CG>(p, fin, hb, 1, code[1], nx[1], ny[1], Ls[1], f, acc);
+  fused_face<SCHEME, VARIANT, false, GHOST_CG>(p, fin, hb, 2, code[2], nx[2], ny[2], Ls[2], f, acc);
+  if (FV) {
+    const float ia = __ldg(p.inv_area + i);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
+  }
+  float* o = fout + cell_base(i, Q);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+}
+
+template <int SCHEME, int VARIANT>
+__device__ __forceinline__ void load_slots(const DevPlan& p, int i, const unsigned*& hb, int code[3],
+                                           float nx[3], float ny[3], float Ls[3]) {
+  constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+  const HfRows HR{3, SCHEME, VARIANT};
+  hb = p.hf + cell_base(i < p.N ? i : 0, HROWS);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    code[k] = int(__ldg(hb + HR.code(k) * 32));
+    nx[k] = __uint_as_float(__ldg(hb + HR.nx(k) * 32));
+    ny[k] = __uint_as_float(__ldg(hb + HR.ny(k) * 32));
+    Ls[k] = __uint_as_float(__ldg(hb + HR.ls(k) * 32));  // L * sigma
+  }
+}
+
 template <int SCHEME, int VARIANT, bool FV>
 __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restrict__ fin,
                                                float* __restrict__ fout, int prefetch_blocks) {
@@ -183,37 +223,84 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
   const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead < int(gridDim.x);
   if (do_prefetch) prefetch_l2(p.hf + size_t(ahead) * 256 * HROWS, 256 * HROWS * sizeof(unsigned));
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const HfRows HR{3, SCHEME, VARIANT};
-  const unsigned* hb = p.hf + cell_base(i < p.N ? i : 0, HROWS);
+  const unsigned* hb;
   int code[3];
-  float nx[3], ny[3], Ls[3];  // Ls = L * sigma
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    code[k] = int(__ldg(hb + HR.code(k) * 32));
-    nx[k] = __uint_as_float(__ldg(hb + HR.nx(k) * 32));
-    ny[k] = __uint_as_float(__ldg(hb + HR.ny(k) * 32));
-    Ls[k] = __uint_as_float(__ldg(hb + HR.ls(k) * 32));
-  }
+  float nx[3], ny[3], Ls[3];
+  load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
   grid_dep_wait();  // fin and the node pdfs come from the previous kernels
   if (do_prefetch) prefetch_l2(fin + size_t(ahead) * 256 * Q, 256 * Q * sizeof(float));
   if (i >= p.N) return;
-  float f[Q];
-  load_cell(fin, i, f);
-  float rho, ux, uy, eq[Q];
-  macros(f, rho, ux, uy);
-  feq9(rho, ux, uy, p, eq);
-  float acc[Q];
-  fused_face<SCHEME, VARIANT, true>(p, fin, hb, 0, code[0], nx[0], ny[0], Ls[0], f, acc);
-  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 1, code[1], nx[1], ny[1], Ls[1], f, acc);
-  fused_face<SCHEME, VARIANT, false>(p, fin, hb, 2, code[2], nx[2], ny[2], Ls[2], f, acc);
-  if (FV) {
-    const float ia = __ldg(p.inv_area + i);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
+  fused_cell<SCHEME, VARIANT, FV, false>(p, fin, fout, i, code, nx, ny, Ls, hb);
+}
+
+// ---------------------------------------------------------------------------
+// Whole step in one launch.  Blocks take tickets in the order they start
+// (atomicAdd after griddepcontrol.wait); the first NB tickets evaluate node
+// blocks and publish them (nodes_done), the others update 256-cell blocks.
+// A cell block that has ghost faces waits (bounded) until every node block
+// has published; since tickets follow start order, every node ticket belongs
+// to a block that is already running, so the wait cannot starve.  The last
+// block to finish resets the counters for the next launch.
+__device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+  return v;
+}
+
+template <int SCHEME, int VARIANT, bool FV>
+__global__ void __launch_bounds__(256) k_step(DevPlan p, const float* __restrict__ fin,
+                                              float* __restrict__ fout, int n_cell_blocks) {
+  static_assert(NODE_BLOCK_ENTRIES == 256, "node blocks use the whole CTA");
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  __shared__ int s_ticket, s_ok;
+  grid_dep_launch();
+  grid_dep_wait();  // fin, and the counters reset by the previous launch
+  int* ctr = p.step_ctr;  // [0] ticket, [1] nodes published, [2] blocks finished
+  if (threadIdx.x == 0) s_ticket = atomicAdd(&ctr[0], 1);
+  __syncthreads();
+  const int t = s_ticket;
+  if (t < p.NB) {
+    node_block<false>(p, fin, t, prod, lastm);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&ctr[1], 1);
+  } else {
+    const int cb = t - p.NB;
+    const int i = cb * 256 + threadIdx.x;
+    const unsigned* hb;
+    int code[3];
+    float nx[3], ny[3], Ls[3];
+    load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
+    if (__ldg(p.cblk_ghost + cb)) {
+      if (threadIdx.x == 0) {
+        int ok = 0;
+        for (int it = 0; it < (1 << 24); ++it) {
+          if (ld_acquire_gpu(&ctr[1]) >= p.NB) {
+            ok = 1;
+            break;
+          }
+          __nanosleep(64);
+        }
+        if (!ok) atomicExch(p.status, STATUS_WAIT_TIMEOUT);
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (s_ok && i < p.N) fused_cell<SCHEME, VARIANT, FV, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
+    } else if (i < p.N) {
+      fused_cell<SCHEME, VARIANT, FV, false>(p, fin, fout, i, code, nx, ny, Ls, hb);
+    }
   }
-  float* o = fout + cell_base(i, Q);
-#pragma unroll
-  for (int q = 0; q < Q; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctr[2], 1) == p.NB + n_cell_blocks - 1) {
+      ctr[0] = 0;
+      ctr[1] = 0;
+      ctr[2] = 0;
+      __threadfence();
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -437,6 +524,25 @@ cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaSt
   if (p.scheme == 1 && p.variant == 0) return fused_dispatch<1, 0>(p, fin, fout, s, pdl);
   if (p.scheme == 0 && p.variant == 1) return fused_dispatch<0, 1>(p, fin, fout, s, pdl);
   if (p.scheme == 1 && p.variant == 1) return fused_dispatch<1, 1>(p, fin, fout, s, pdl);
+  return cudaErrorInvalidValue;
+}
+
+template <int S, int V>
+static cudaError_t step_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
+                                 bool pdl) {
+  const int ncb = blocks(p.N, 256);
+  const int g = p.NB + ncb;
+  if (p.fv) return launch_ex(k_step<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, ncb);
+  return launch_ex(k_step<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, ncb);
+}
+
+cudaError_t launch_step(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl) {
+  if (p.N == 0) return cudaSuccess;
+  if (p.K != 3) return cudaErrorInvalidValue;
+  if (p.scheme == 0 && p.variant == 0) return step_dispatch<0, 0>(p, fin, fout, s, pdl);
+  if (p.scheme == 1 && p.variant == 0) return step_dispatch<1, 0>(p, fin, fout, s, pdl);
+  if (p.scheme == 0 && p.variant == 1) return step_dispatch<0, 1>(p, fin, fout, s, pdl);
+  if (p.scheme == 1 && p.variant == 1) return step_dispatch<1, 1>(p, fin, fout, s, pdl);
   return cudaErrorInvalidValue;
 }
 

@@ -420,6 +420,13 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       if (pr.variant == 1) hp.hf[hfi(i, HR.sc(k))] = fbits(hp.fscale[j]);
     }
   }
+  if (hp.fusable) {
+    hp.cblk_ghost.assign((N + 255) / 256, 0);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < K; ++k)
+        if (hp.hf[hfi(i, HR.code(k))] & HF_GHOST) hp.cblk_ghost[i / 256] = 1;
+  }
+
   // ---- tile tables: per tile the nodes its ghost faces need (plus owner-only
   // computed nodes that no ghost face uses), their stencil entries, and the
   // ghost end nodes as tile-local indices

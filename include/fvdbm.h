@@ -63,6 +63,7 @@ extern "C" {
 #define FVDBM_KERNEL_FUSED 2      /* node BC + fused cell kernel (2 kernels) */
 #define FVDBM_KERNEL_TILE 3       /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
 #define FVDBM_KERNEL_TILE_SPLIT 4 /* node BC kernel + persistent tile kernel (2 kernels) */
+#define FVDBM_KERNEL_ONE 5        /* node and cell blocks in one launch (1 kernel) */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {

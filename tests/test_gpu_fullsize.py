@@ -68,7 +68,7 @@ def test_channel_config_bitwise(flux):
     from fvdbm_jax_gb300 import Environment, meshgen
     m, dyn, c, f, n = _case(meshgen.channel_cylinder(), flux, tau=0.55, bc="channel")
     ref = _oracle(c, f, n, dyn, 100)
-    for kernel in ("tile", "tile_split", "fused", "staged"):
+    for kernel in ("one", "tile", "tile_split", "fused", "staged"):
         env = Environment(c, f, n, kernel=kernel)
         env.init()
         env.step(100)
@@ -91,7 +91,7 @@ def test_porous_1m_bitwise_and_deterministic():
     env2.init()
     env2.step(4)
     assert np.array_equal(np.array(env2.cells.pdf), a)
-    for kernel in ("fused", "tile_split"):
+    for kernel in ("one", "fused", "tile_split"):
         env3 = Environment(c, f, n, kernel=kernel)
         env3.init()
         env3.step(4)
