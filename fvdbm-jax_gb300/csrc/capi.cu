@@ -377,7 +377,10 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   CR(cudaMemsetAsync(h->status, 0, 4 * sizeof(int), h->stream));
   p.status = h->status;
   p.step_ctr = h->status + 1;
-  if (h->fused) UP(cblk_ghost, hp.cblk_ghost);
+  if (h->fused) {
+    UP(cblk_ghost, hp.cblk_ghost);
+    UP(sched, hp.sched);
+  }
   if (h->tile) CR(prepare_tile(p));
   {
     float* d = nullptr;

@@ -88,6 +88,7 @@ struct HostPlan {
   // NODE_BLOCK_ENTRIES stencil entries each; nb_meta = 4 ints per block
   std::vector<int32_t> nb_ptr, nb_meta;
   std::vector<uint8_t> cblk_ghost;  // per 256-cell block: any ghost face
+  std::vector<int32_t> sched;       // single-launch tickets: cell block >= 0, node block -(b+1)
 
   // nodes on the device: computed (type 1/2) first, then frozen ghost ends
   int M = 0, Mc = 0, Mp = 0;
@@ -187,6 +188,7 @@ struct DevPlan {
   int* status;  // device status word (0 ok); set when a bounded wait gives up
   int* step_ctr;  // single-launch step: ticket, node blocks published, blocks finished
   const unsigned char* cblk_ghost;  // per 256-cell block: has a ghost face
+  const int* sched;                 // single-launch tickets: cell block >= 0, node block -(b+1)
 };
 
 constexpr int STATUS_WAIT_TIMEOUT = 1;

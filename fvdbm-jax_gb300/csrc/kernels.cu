@@ -235,12 +235,14 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
 
 // ---------------------------------------------------------------------------
 // Whole step in one launch.  Blocks take tickets in the order they start
-// (atomicAdd after griddepcontrol.wait); the first NB tickets evaluate node
-// blocks and publish them (nodes_done), the others update 256-cell blocks.
-// A cell block that has ghost faces waits (bounded) until every node block
-// has published; since tickets follow start order, every node ticket belongs
-// to a block that is already running, so the wait cannot starve.  The last
-// block to finish resets the counters for the next launch.
+// (atomicAdd after griddepcontrol.wait); a static schedule maps each ticket
+// to a node block or a 256-cell block.  Node blocks are interleaved with the
+// ghost-free cell blocks (their latency overlaps cell work) and publish their
+// results (nodes_done); the cell blocks with ghost faces come last and wait
+// (bounded) until every node block has published.  Tickets follow start
+// order, so every node ticket before a waiting block belongs to a block that
+// is already running: the wait cannot starve.  The last block to finish
+// resets the counters for the next launch.
 __device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
   int v;
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
@@ -249,7 +251,8 @@ __device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
 
 template <int SCHEME, int VARIANT, bool FV>
 __global__ void __launch_bounds__(256) k_step(DevPlan p, const float* __restrict__ fin,
-                                              float* __restrict__ fout, int n_cell_blocks) {
+                                              float* __restrict__ fout, int n_cell_blocks,
+                                              int prefetch_blocks) {
   static_assert(NODE_BLOCK_ENTRIES == 256, "node blocks use the whole CTA");
   __shared__ float prod[12][NODE_BLOCK_ENTRIES];
   __shared__ float lastm[3];
@@ -260,13 +263,25 @@ __global__ void __launch_bounds__(256) k_step(DevPlan p, const float* __restrict
   if (threadIdx.x == 0) s_ticket = atomicAdd(&ctr[0], 1);
   __syncthreads();
   const int t = s_ticket;
-  if (t < p.NB) {
-    node_block<false>(p, fin, t, prod, lastm);
+  const int work = __ldg(p.sched + t);
+  if (work < 0) {
+    node_block<false>(p, fin, -work - 1, prod, lastm);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) atomicAdd(&ctr[1], 1);
   } else {
-    const int cb = t - p.NB;
+    constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+    const int cb = work;
+    // the cell block about one wave ahead in ticket order streams into L2
+    const int ta = t + prefetch_blocks;
+    if (threadIdx.x == 0 && ta < p.NB + n_cell_blocks) {
+      const int wa = __ldg(p.sched + ta);
+      if (wa >= 0) {
+        const size_t c0 = size_t(wa) * 256;
+        prefetch_l2(fin + c0 * Q, 256 * Q * sizeof(float));
+        prefetch_l2(p.hf + c0 * HROWS, 256 * HROWS * sizeof(unsigned));
+      }
+    }
     const int i = cb * 256 + threadIdx.x;
     const unsigned* hb;
     int code[3];
@@ -532,8 +547,9 @@ static cudaError_t step_dispatch(const DevPlan& p, const float* fin, float* fout
                                  bool pdl) {
   const int ncb = blocks(p.N, 256);
   const int g = p.NB + ncb;
-  if (p.fv) return launch_ex(k_step<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, ncb);
-  return launch_ex(k_step<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, ncb);
+  const int pf = fused_prefetch_blocks();
+  if (p.fv) return launch_ex(k_step<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, ncb, pf);
+  return launch_ex(k_step<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, ncb, pf);
 }
 
 cudaError_t launch_step(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl) {

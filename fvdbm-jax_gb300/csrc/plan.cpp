@@ -206,6 +206,17 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     std::iota(hp.cell_old.begin(), hp.cell_old.end(), 0);
     if (pr.ordering == FVDBM_ORDER_MORTON) hp.ordering = FVDBM_ORDER_NONE;
   }
+  // cells with a ghost face go last (stable), so that the blocks of the
+  // single-launch step that need boundary nodes form the tail of the grid
+  if (N > 0 && K > 0 && F > 0) {
+    std::vector<char> has_ghost(N, 0);
+    for (int c = 0; c < N; ++c)
+      for (int k = 0; k < K; ++k) {
+        const int f = wrap(m.cell_face_indices[int64_t(c) * K + k], F);
+        if (m.face_cells[2 * f] == -1 || m.face_cells[2 * f + 1] == -1) has_ghost[c] = 1;
+      }
+    std::stable_partition(hp.cell_old.begin(), hp.cell_old.end(), [&](int32_t c) { return !has_ghost[c]; });
+  }
   hp.cell_new.assign(N, -1);
   for (int i = 0; i < N; ++i) hp.cell_new[hp.cell_old[i]] = i;
   hp.last_cell_new = N > 0 ? hp.cell_new[N - 1] : 0;
@@ -503,6 +514,27 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     }
     hp.NT = NT;
     hp.tile_ok = ok;
+  }
+
+  // single-launch schedule: ticket -> work item (>= 0 cell block, < 0 node
+  // block -(b+1)).  Node blocks are spread evenly over the first two thirds of
+  // the ghost-free cell blocks; the cell blocks with ghost faces come last.
+  if (hp.fusable && N > 0) {
+    std::vector<int32_t> free_blocks, ghost_blocks;
+    for (int b = 0; b < int(hp.cblk_ghost.size()); ++b)
+      (hp.cblk_ghost[b] ? ghost_blocks : free_blocks).push_back(b);
+    const int NBk = int(hp.nb_meta.size() / 4);
+    const int64_t span = std::max<int64_t>(1, (int64_t(free_blocks.size()) * 2) / 3);
+    hp.sched.clear();
+    int nb_next = 0;
+    for (size_t j = 0; j < free_blocks.size(); ++j) {
+      // node blocks due before this cell block
+      const int64_t due = std::min<int64_t>(NBk, (int64_t(j) * NBk + span - 1) / span);
+      while (nb_next < due) hp.sched.push_back(-(nb_next++ + 1));
+      hp.sched.push_back(free_blocks[j]);
+    }
+    while (nb_next < NBk) hp.sched.push_back(-(nb_next++ + 1));
+    for (int32_t b : ghost_blocks) hp.sched.push_back(b);
   }
 
   if (hp.fv) {
