@@ -165,7 +165,10 @@ int enqueue_steps(Handle* h, int n) {
       if (!h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
       CK(launch_tile(h->dp, fin, fout, h->stream));
     } else {
-      CK(launch_nodes(h->dp, fin, h->stream, /*pdl=*/s > 0));
+      if (h->fused)
+        CK(launch_nodes_cp(h->dp, fin, h->stream, /*pdl=*/s > 0));
+      else
+        CK(launch_nodes(h->dp, fin, h->stream, /*pdl=*/s > 0));
       if (h->fused) {
         CK(launch_fused(h->dp, fin, fout, h->stream, /*pdl=*/h->dp.NB > 0 || s > 0));
       } else {
@@ -295,7 +298,7 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
              "naming a face of that cell, and no per-q flux scale";
     return create_fail(h, FVDBM_EINVAL);
   }
-  h->one = one_possible && (params->kernel == FVDBM_KERNEL_ONE || params->kernel == FVDBM_KERNEL_AUTO);
+  h->one = one_possible && params->kernel == FVDBM_KERNEL_ONE;
   h->dp.tile_nodes = (params->kernel == FVDBM_KERNEL_TILE) ? 1 : 0;
   p.N = hp.N;
   p.Np = hp.Np;
@@ -357,6 +360,17 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   UP(nd_sumw, hp.nd_sumw);
   UP(nb_meta, hp.nb_meta);
   p.NB = int(hp.nb_meta.size() / 4);
+  UP(pe_slot, hp.pe_slot);
+  UP(pe_w, hp.pe_w);
+  UP(pn_meta, hp.pn_meta);
+  UP(pn_sumw, hp.pn_sumw);
+  p.stencil_start = hp.stencil_start;
+  p.Sp = std::max(32, (hp.N - hp.stencil_start + 31) / 32 * 32);
+  {
+    float* d = nullptr;
+    if ((rc = dalloc<float>(h, &d, size_t(12) * p.Sp)) != FVDBM_OK) return create_fail(h, rc);
+    p.cprod = d;
+  }
   UP(inv_area, hp.inv_area);
   p.NT = hp.NT;
   if (h->tile) {
@@ -435,6 +449,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
   if (cell_pdf && hp.N > 0) {
     CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(Q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
     CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream));
+    if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
   }
   if (node_pdf || node_rho || node_vel) {
     if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(Q) * hp.P * 4);
@@ -494,7 +509,10 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
   if (phase == 1) {
-    if (!h->one && (!h->tile || !h->dp.tile_nodes)) CK(launch_nodes(h->dp, fin, h->stream));
+    if (h->fused && !h->one && !h->tile)
+      CK(launch_nodes_cp(h->dp, fin, h->stream, false));
+    else if (!h->one && (!h->tile || !h->dp.tile_nodes))
+      CK(launch_nodes(h->dp, fin, h->stream));
   } else if (phase == 2) {
     if (h->one) {
       CK(launch_step(h->dp, fin, fout, h->stream, false));

@@ -87,6 +87,10 @@ struct HostPlan {
   // node blocks of the node kernel: contiguous computed nodes with at most
   // NODE_BLOCK_ENTRIES stencil entries each; nb_meta = 4 ints per block
   std::vector<int32_t> nb_ptr, nb_meta;
+  std::vector<uint32_t> pe_slot;  // padded node-block tables (see plan.cpp)
+  std::vector<float> pe_w, pn_sumw;
+  std::vector<int32_t> pn_meta;
+  int stencil_start = 0;  // device cells [stencil_start, N) are node-stencil cells
   std::vector<uint8_t> cblk_ghost;  // per 256-cell block: any ghost face
   std::vector<int32_t> sched;       // single-launch tickets: cell block >= 0, node block -(b+1)
 
@@ -166,6 +170,14 @@ struct DevPlan {
   const float* nd_sumw;
   const int* nb_meta;  // node blocks: {first node, end node, first entry, end entry}
   int NB;
+  // macros of the node-stencil cells [stencil_start, N): cprod[r][Sp] with
+  // r = rho, ux, uy, f_q - feq_q; written by the fused kernel for the next step
+  int stencil_start, Sp;
+  float* cprod;
+  const unsigned* pe_slot;
+  const float* pe_w;
+  const int* pn_meta;
+  const float* pn_sumw;
   float* node_pdf;  // [9][Mp]
   float* node_rho;  // [Mp]
   float* node_vel;  // [2][Mp]
@@ -198,6 +210,10 @@ constexpr int STATUS_WAIT_TIMEOUT = 1;
 cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s, bool pdl = false);
 cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
                          bool pdl = false);
+// node kernel fed by the stencil macros the previous fused kernel recorded
+cudaError_t launch_nodes_cp(const DevPlan& p, const float* f, cudaStream_t s, bool pdl);
+// record the stencil macros of f (after an upload of the cell pdfs)
+cudaError_t launch_stencil_macros(const DevPlan& p, const float* f, cudaStream_t s);
 // the whole step in one launch (node blocks then cell blocks, see kernels.cu)
 cudaError_t launch_step(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl);
 cudaError_t launch_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);

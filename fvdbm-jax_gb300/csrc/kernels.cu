@@ -11,6 +11,20 @@
 
 namespace fvdbm {
 
+// Macros of a node-stencil cell for the next step's node kernel:
+// rho, ux, uy, f_q - feq_q (src/containers.py:93-105,388-390).
+__device__ __forceinline__ void record_stencil(const DevPlan& p, int i, const float fn[Q]) {
+  float rho, ux, uy, eq[Q];
+  macros(fn, rho, ux, uy);
+  feq9(rho, ux, uy, p, eq);
+  float* c = p.cprod + (i - p.stencil_start);
+  c[0] = rho;
+  c[size_t(p.Sp)] = ux;
+  c[2 * size_t(p.Sp)] = uy;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) c[(3 + q) * size_t(p.Sp)] = fn[q] - eq[q];
+}
+
 // ---------------------------------------------------------------------------
 // Boundary nodes: Nodes.calc_pdfs (src/containers.py:339-404).  A block holds
 // whole nodes with at most NODE_BLOCK_ENTRIES stencil entries:
@@ -117,6 +131,92 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
   node_block<true>(p, f, blockIdx.x, prod, lastm);
 }
 
+// The same node evaluation, fed by the stencil macros that the previous
+// fused kernel recorded (cprod) instead of re-reading the stencil pdfs.  The
+// padded tables put a thread's entry and node record at blk*256 + tid, so the
+// first loads do not depend on one another.
+__global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes_cp(DevPlan p, const float* __restrict__ f) {
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  grid_dep_launch();
+  const int tid = threadIdx.x;
+  const size_t s = size_t(blockIdx.x) * NODE_BLOCK_ENTRIES + tid;
+  const unsigned slot = __ldg(p.pe_slot + s);
+  const float w = __ldg(p.pe_w + s);
+  const int4 nm = __ldg(reinterpret_cast<const int4*>(p.pn_meta) + s);  // node, first, count, type|npad
+  const float sw = __ldg(p.pn_sumw + s);
+  const int type = nm.w & 3;
+  float set0 = 0.0f, set1 = 0.0f;
+  if (type == 1) {
+    set0 = p.node_vel[nm.x];
+    set1 = p.node_vel[p.Mp + nm.x];
+  } else if (type == 2) {
+    set0 = p.node_rho[nm.x];
+  }
+  grid_dep_wait();  // cprod comes from the previous fused kernel
+  if (slot != ~0u) {
+    const float* c = p.cprod + (slot & ~ND_NEQ_ZERO);
+    const bool zero = (slot & ND_NEQ_ZERO) != 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) prod[r][tid] = __ldg(c + r * size_t(p.Sp)) * w;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) prod[3 + q][tid] = (zero ? 0.0f : __ldg(c + (3 + q) * size_t(p.Sp))) * w;
+  }
+  if (tid == NODE_BLOCK_ENTRIES - 1) {
+    // padded (-1, weight 0) entries gather the last cell
+    float fc[Q];
+    load_cell(f, p.last_cell, fc);
+    float rho, ux, uy;
+    macros(fc, rho, ux, uy);
+    lastm[0] = rho;
+    lastm[1] = ux;
+    lastm[2] = uy;
+  }
+  __syncthreads();
+  if (type == 0) return;
+  const int b = nm.y, cnt = nm.z;
+  float acc[12];
+#pragma unroll
+  for (int r = 0; r < 12; ++r) acc[r] = 0.0f;
+  for (int k = 0; k < cnt; ++k) {
+#pragma unroll
+    for (int r = 0; r < 12; ++r) acc[r] = k ? acc[r] + prod[r][b + k] : prod[r][b + k];
+  }
+  if (nm.w & 4) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const float z = lastm[r] * 0.0f;
+      acc[r] = cnt ? acc[r] + z : z;
+    }
+  }
+  const int m = nm.x;
+  float rho_p, ux_p, uy_p;
+  if (type == 1) {
+    rho_p = acc[0] / sw;
+    ux_p = set0;
+    uy_p = set1;
+    p.node_rho[m] = rho_p;
+  } else {
+    rho_p = set0;
+    ux_p = acc[1] / sw;
+    uy_p = acc[2] / sw;
+    p.node_vel[m] = ux_p;
+    p.node_vel[p.Mp + m] = uy_p;
+  }
+  float eqn[Q];
+  feq9(rho_p, ux_p, uy_p, p, eqn);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) p.node_pdf[size_t(q) * p.Mp + m] = eqn[q] + acc[3 + q] / sw;
+}
+
+__global__ void __launch_bounds__(256) k_stencil_macros(DevPlan p, const float* __restrict__ f) {
+  const int i = p.stencil_start + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  float fc[Q];
+  load_cell(f, i, fc);
+  record_stencil(p, i, fc);
+}
+
 // ---------------------------------------------------------------------------
 // Fused cell kernel: macros, feq, the flux of each of the cell's faces
 // (recomputed from the canonical slot-0/slot-1 pair, so both neighbours get
@@ -173,8 +273,9 @@ __device__ __forceinline__ void prefetch_l2(const void* ptr, uint32_t bytes) {
 }
 
 // One cell of the fused update.  GHOST_CG: read node pdfs through L2 (they
-// were written earlier in the same launch).
-template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG>
+// were written earlier in the same launch).  RECORD: node-stencil cells also
+// record the macros of their new pdfs.
+template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG, bool RECORD = false>
 __device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __restrict__ fin,
                                            float* __restrict__ fout, int i, const int code[3],
                                            const float nx[3], const float ny[3], const float Ls[3],
@@ -194,8 +295,13 @@ __device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __rest
     for (int q = 0; q < Q; ++q) acc[q] = acc[q] * ia;
   }
   float* o = fout + cell_base(i, Q);
+  float fn[Q];
 #pragma unroll
-  for (int q = 0; q < Q; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+  for (int q = 0; q < Q; ++q) {
+    fn[q] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+    o[q * 32] = fn[q];
+  }
+  if (RECORD && i >= p.stencil_start) record_stencil(p, i, fn);
 }
 
 template <int SCHEME, int VARIANT>
@@ -230,7 +336,7 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
   grid_dep_wait();  // fin and the node pdfs come from the previous kernels
   if (do_prefetch) prefetch_l2(fin + size_t(ahead) * 256 * Q, 256 * Q * sizeof(float));
   if (i >= p.N) return;
-  fused_cell<SCHEME, VARIANT, FV, false>(p, fin, fout, i, code, nx, ny, Ls, hb);
+  fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
 }
 
 // ---------------------------------------------------------------------------
@@ -510,6 +616,18 @@ static cudaError_t launch_ex(void (*kern)(KArgs...), int grid, int block, size_t
 cudaError_t launch_nodes(const DevPlan& p, const float* f, cudaStream_t s, bool pdl) {
   if (p.NB == 0) return cudaSuccess;
   return launch_ex(k_nodes, p.NB, NODE_BLOCK_ENTRIES, 0, s, pdl, p, f);
+}
+
+cudaError_t launch_nodes_cp(const DevPlan& p, const float* f, cudaStream_t s, bool pdl) {
+  if (p.NB == 0) return cudaSuccess;
+  return launch_ex(k_nodes_cp, p.NB, NODE_BLOCK_ENTRIES, 0, s, pdl, p, f);
+}
+
+cudaError_t launch_stencil_macros(const DevPlan& p, const float* f, cudaStream_t s) {
+  const int S = p.N - p.stencil_start;
+  if (S <= 0) return cudaSuccess;
+  k_stencil_macros<<<blocks(S, 256), 256, 0, s>>>(p, f);
+  return cudaGetLastError();
 }
 
 static int fused_prefetch_blocks() {

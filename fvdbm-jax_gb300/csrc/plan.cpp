@@ -206,16 +206,27 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     std::iota(hp.cell_old.begin(), hp.cell_old.end(), 0);
     if (pr.ordering == FVDBM_ORDER_MORTON) hp.ordering = FVDBM_ORDER_NONE;
   }
-  // cells with a ghost face go last (stable), so that the blocks of the
-  // single-launch step that need boundary nodes form the tail of the grid
-  if (N > 0 && K > 0 && F > 0) {
-    std::vector<char> has_ghost(N, 0);
-    for (int c = 0; c < N; ++c)
-      for (int k = 0; k < K; ++k) {
-        const int f = wrap(m.cell_face_indices[int64_t(c) * K + k], F);
-        if (m.face_cells[2 * f] == -1 || m.face_cells[2 * f + 1] == -1) has_ghost[c] = 1;
+  // the stencil cells of the computed boundary nodes go last (stable): the
+  // fused kernel's tail blocks then also record their macros for the next
+  // step's node kernel, and the blocks that need boundary nodes in the
+  // single-launch step form the tail of its grid.  (Not for the in-tile node
+  // kernel, whose tiles must stay compact.)
+  hp.stencil_start = N;
+  if (N > 0 && Kn > 0 && pr.kernel != FVDBM_KERNEL_TILE) {
+    std::vector<char> member(N, 0);
+    for (int p_ = 0; p_ < P; ++p_) {
+      if (m.node_type[p_] == 0) continue;
+      for (int k = 0; k < Kn; ++k) {
+        const int32_t c = m.node_cells[int64_t(p_) * Kn + k];
+        float w = 1.0f / m.node_dists[int64_t(p_) * Kn + k];
+        if (w < 0.0f) w = 0.0f;
+        if (c == -1 && w == 0.0f) continue;  // padding: evaluated from the last cell directly
+        member[wrap(c, N)] = 1;
       }
-    std::stable_partition(hp.cell_old.begin(), hp.cell_old.end(), [&](int32_t c) { return !has_ghost[c]; });
+    }
+    auto it = std::stable_partition(hp.cell_old.begin(), hp.cell_old.end(),
+                                    [&](int32_t c) { return !member[c]; });
+    hp.stencil_start = int(it - hp.cell_old.begin());
   }
   hp.cell_new.assign(N, -1);
   for (int i = 0; i < N; ++i) hp.cell_new[hp.cell_old[i]] = i;
@@ -309,6 +320,38 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     hp.nb_meta.push_back(hp.nb_ptr[b + 1]);
     hp.nb_meta.push_back(hp.nd_ptr[hp.nb_ptr[b]]);
     hp.nb_meta.push_back(hp.nd_ptr[hp.nb_ptr[b + 1]]);
+  }
+  // the same blocks, padded to NODE_BLOCK_ENTRIES slots so that a thread's
+  // entry and node record sit at blk*NODE_BLOCK_ENTRIES + tid:
+  //   pe_slot  stencil slot of the entry's cell (| ND_NEQ_ZERO), or ~0u
+  //   pe_w     weight
+  //   pn_meta  {node, first local entry, entry count, type | npad << 2}, type 0 = empty
+  //   pn_sumw  sum of weights
+  {
+    const int NBk = int(hp.nb_meta.size() / 4);
+    hp.pe_slot.assign(size_t(NBk) * NODE_BLOCK_ENTRIES, ~0u);
+    hp.pe_w.assign(size_t(NBk) * NODE_BLOCK_ENTRIES, 0.0f);
+    hp.pn_meta.assign(size_t(NBk) * NODE_BLOCK_ENTRIES * 4, 0);
+    hp.pn_sumw.assign(size_t(NBk) * NODE_BLOCK_ENTRIES, 0.0f);
+    for (int b = 0; b < NBk; ++b) {
+      const int n0 = hp.nb_meta[4 * b], n1 = hp.nb_meta[4 * b + 1], e0 = hp.nb_meta[4 * b + 2];
+      for (int j = 0; j < n1 - n0; ++j) {
+        const int d = n0 + j;
+        const size_t s = size_t(b) * NODE_BLOCK_ENTRIES + j;
+        hp.pn_meta[4 * s + 0] = d;
+        hp.pn_meta[4 * s + 1] = hp.nd_ptr[d] - e0;
+        hp.pn_meta[4 * s + 2] = hp.nd_ptr[d + 1] - hp.nd_ptr[d];
+        hp.pn_meta[4 * s + 3] = hp.nd_type[d] | (hp.nd_npad[d] > 0 ? 4 : 0);
+        hp.pn_sumw[s] = hp.nd_sumw[d];
+      }
+      for (int e = hp.nd_ptr[n0]; e < hp.nd_ptr[n1]; ++e) {
+        const size_t s = size_t(b) * NODE_BLOCK_ENTRIES + (e - e0);
+        const uint32_t code = hp.nd_cell[e];
+        const int32_t cell = int32_t(code & ~ND_NEQ_ZERO);
+        hp.pe_slot[s] = uint32_t(cell - hp.stencil_start) | (code & ND_NEQ_ZERO);
+        hp.pe_w[s] = hp.nd_w[e];
+      }
+    }
   }
 
   // ---- faces in device order (by lowest slot cell)
