@@ -56,7 +56,8 @@ class Info(C.Structure):
 _LIB = None
 EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", "fvdbm_get_cells", "fvdbm_get_nodes",
            "fvdbm_get_face_fluxes", "fvdbm_sync", "fvdbm_stream", "fvdbm_get_info",
-           "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check"]
+           "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check",
+           "fvdbm_step_static_scratch"]
 
 
 def lib_path() -> str:
@@ -77,6 +78,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_set_state.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]
     L.fvdbm_step.argtypes = [vp, C.c_int32]
     L.fvdbm_step_phase.argtypes = [vp, C.c_int32]
+    L.fvdbm_step_static_scratch.argtypes = [vp, C.c_int32]
     L.fvdbm_get_cells.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]
     L.fvdbm_get_nodes.argtypes = [vp, _f32p, _f32p, _f32p]
     L.fvdbm_get_face_fluxes.argtypes = [vp, _f32p]

@@ -657,3 +657,74 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Staged step with a fixed face-flux scratch array.  For callers that cannot
+// allocate device memory while they step: a host framework that owns the
+// device's memory (JAX/XLA preallocates most of it by default), or a loop in
+// which a cudaMalloc/cudaFree would stall the device.  The array is shared by
+// every call on a device and keeps the last call's fluxes; nothing in it needs
+// to start at zero, because each step's face kernel writes all 9 x F fluxes
+// before the gather reads any of them.  Calls whose kernels overlap on the GPU
+// race on the array.
+
+static __device__ __align__(256) float g_face_flux_scratch[size_t(Q) * FVDBM_STATIC_SCRATCH_MAX_FACES];
+
+namespace {
+
+constexpr int kScratchDevices = 64;
+std::mutex g_scratch_mu;
+float* g_scratch_addr[kScratchDevices] = {};
+
+// Device address of the scratch array on h's device (current on entry),
+// looked up on the first call for that device.
+int scratch_address(Handle* h, float** out) {
+  if (h->device < 0 || h->device >= kScratchDevices)
+    return fail(h, FVDBM_EINVAL, "fvdbm_step_static_scratch: device index " + std::to_string(h->device) +
+                                     " out of range");
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch_addr[h->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_face_flux_scratch);
+    if (e != cudaSuccess)
+      return fail(h, FVDBM_ECUDA, std::string("cudaGetSymbolAddress(face flux scratch): ") +
+                                      cudaGetErrorString(e));
+    g_scratch_addr[h->device] = static_cast<float*>(p);
+  }
+  *out = g_scratch_addr[h->device];
+  return FVDBM_OK;
+}
+
+}  // namespace
+
+extern "C" int fvdbm_step_static_scratch(void* handle, int32_t n_steps) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  if (n_steps < 0) return fail(h, FVDBM_EINVAL, "n_steps < 0");
+  if (h->fused || h->tile || h->one)
+    return fail(h, FVDBM_EINVAL,
+                "fvdbm_step_static_scratch steps the staged kernels only: create the handle with "
+                "FVDBM_KERNEL_STAGED");
+  if (hp.Fp > FVDBM_STATIC_SCRATCH_MAX_FACES)
+    return fail(h, FVDBM_EINVAL,
+                "fvdbm_step_static_scratch: the mesh has " + std::to_string(hp.F) + " faces (" +
+                    std::to_string(hp.Fp) + " padded); the static face-flux scratch holds at most " +
+                    std::to_string(FVDBM_STATIC_SCRATCH_MAX_FACES) + " padded faces (" +
+                    std::to_string(size_t(Q) * FVDBM_STATIC_SCRATCH_MAX_FACES * 4) +
+                    " bytes); use fvdbm_step");
+  CK(cudaSetDevice(h->device));
+  float* scratch = nullptr;
+  int rc = scratch_address(h, &scratch);
+  if (rc != FVDBM_OK) return rc;
+  for (int s = 0; s < n_steps; ++s) {
+    const float* fin = h->f[h->cur];
+    float* fout = h->f[h->cur ^ 1];
+    CK(launch_nodes(h->dp, fin, h->stream));
+    CK(launch_face_flux(h->dp, fin, scratch, h->stream));
+    CK(launch_gather(h->dp, fin, scratch, fout, h->stream));
+    h->cur ^= 1;
+  }
+  h->steps_done += n_steps;
+  return FVDBM_OK;
+}

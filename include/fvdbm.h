@@ -180,6 +180,34 @@ int fvdbm_destroy(void *handle);
 
 int fvdbm_abi_version(void);
 
+/* Largest padded face count (faces rounded up to a multiple of 128, at least
+ * 128) that fvdbm_step_static_scratch takes: its face-flux scratch is a fixed
+ * device array of 9 x 131072 float32 = 4.5 MiB per device. */
+#define FVDBM_STATIC_SCRATCH_MAX_FACES 131072
+
+/* No counterpart in the reference.  n_steps steps of the staged kernels
+ * (boundary nodes, per-face fluxes, per-cell gather and update) like
+ * fvdbm_step on a handle created with FVDBM_KERNEL_STAGED, with the same
+ * results, but with the per-step face fluxes in a fixed device array of the
+ * library instead of the handle's buffer, and with no device memory
+ * allocated or freed during the call: for callers that cannot allocate
+ * device memory while they step, because another allocator owns the
+ * device's memory (JAX/XLA preallocates most of it by default, so the
+ * reference's own process has little left) or because a cudaMalloc or
+ * cudaFree there would stall the device (cudaFree synchronises it).
+ * Only handles created with FVDBM_KERNEL_STAGED (or that the fused kernels
+ * refused) are accepted; meshes whose padded face count exceeds
+ * FVDBM_STATIC_SCRATCH_MAX_FACES are rejected with FVDBM_EINVAL and a
+ * message, before any work is queued.  The first call on a device looks up
+ * the array's device address (once per device, under a lock); make that
+ * first call before any stream capture.  Every call on a device shares the
+ * one array and leaves its last fluxes there (no part of it needs to start
+ * at zero: each step writes every face before it reads one); calls whose
+ * kernels overlap on the GPU (other streams, other handles, other threads)
+ * race on it, so order them on one stream or with events.  Asynchronous,
+ * like fvdbm_step. */
+int fvdbm_step_static_scratch(void *handle, int32_t n_steps);
+
 #ifdef __cplusplus
 }
 #endif
