@@ -30,7 +30,7 @@ class Mesh(C.Structure):
         ("face_cells", _i32p), ("face_dists", _f32p), ("face_nodes", _i32p),
         ("face_n", _f32p), ("face_L", _f32p), ("face_scale", _f32p),
         ("node_type", _i32p), ("node_cells", _i32p), ("node_dists", _f32p),
-        ("cell_xy", _f32p), ("cell_inv_area", _f32p),
+        ("cell_xy", _f32p), ("cell_inv_area", _f32p), ("cell_area", _f32p),
     ]
 
 
@@ -57,7 +57,7 @@ _LIB = None
 EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", "fvdbm_get_cells", "fvdbm_get_nodes",
            "fvdbm_get_face_fluxes", "fvdbm_sync", "fvdbm_stream", "fvdbm_get_info",
            "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check",
-           "fvdbm_step_static_scratch"]
+           "fvdbm_step_static_scratch", "fvdbm_residual", "fvdbm_run_to_steady"]
 
 
 def lib_path() -> str:
@@ -79,6 +79,9 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_step.argtypes = [vp, C.c_int32]
     L.fvdbm_step_phase.argtypes = [vp, C.c_int32]
     L.fvdbm_step_static_scratch.argtypes = [vp, C.c_int32]
+    L.fvdbm_residual.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.fvdbm_run_to_steady.argtypes = [vp, C.c_double, C.c_int32, C.c_int64, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_double)]
     L.fvdbm_get_cells.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]
     L.fvdbm_get_nodes.argtypes = [vp, _f32p, _f32p, _f32p]
     L.fvdbm_get_face_fluxes.argtypes = [vp, _f32p]
@@ -93,7 +96,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_const_div_check.argtypes = [C.c_int32, C.c_float, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
     for name in EXPORTS:
         getattr(L, name)
-    if L.fvdbm_abi_version() != 1:
+    if L.fvdbm_abi_version() != 2:
         raise RuntimeError("libfvdbm ABI version mismatch")
     _LIB = L
     return L

@@ -40,8 +40,15 @@ struct Handle {
   int* status = nullptr;
   std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // convergence monitor (fvdbm_residual)
+  float* usnap = nullptr;   // [2][Np] velocity at the previous residual call
+  double* red = nullptr;    // chunk partials, then the 4 totals
+  float* d_area = nullptr;  // [Np] cell areas (mass weights) or null
+  long long snap_step = -1; // steps_done at the snapshot, -1 = none
   std::string err;
 };
+
+constexpr int kResidualChunk = 1024;  // cells per partial sum of the monitor
 
 // Known-divisor division (see cdiv in kernels.cu) is used only for divisors
 // whose exhaustive check on this device found no dividend that it rounds
@@ -396,6 +403,8 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
     UP(sched, hp.sched);
   }
   if (h->tile) CR(prepare_tile(p));
+  if (!hp.area.empty())
+    if ((rc = dalloc(h, &h->d_area, hp.area.size(), &hp.area)) != FVDBM_OK) return create_fail(h, rc);
   {
     float* d = nullptr;
     if ((rc = dalloc<float>(h, &d, size_t(Q) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
@@ -450,6 +459,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
     CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(Q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
     CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream));
     if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
+    h->snap_step = -1;
   }
   if (node_pdf || node_rho || node_vel) {
     if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(Q) * hp.P * 4);
@@ -629,6 +639,60 @@ int fvdbm_get_face_fluxes(void* handle, float* flux) {
     const int f = hp.face_old[j];
     for (int q = 0; q < Q; ++q) flux[size_t(f) * Q + q] = soa[size_t(q) * hp.Fp + j];
   }
+  return FVDBM_OK;
+}
+
+int fvdbm_residual(void* handle, double* res_u, double* mass) {
+  if (!handle || !res_u || !mass) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  const int nb = residual_chunks(hp.N, kResidualChunk);
+  if (!h->usnap) {
+    int rc = dalloc<float>(h, &h->usnap, size_t(2) * hp.Np);
+    if (rc != FVDBM_OK) return rc;
+    if ((rc = dalloc<double>(h, &h->red, size_t(4) * (nb + 1))) != FVDBM_OK) return rc;
+  }
+  const bool have = h->snap_step >= 0;
+  double* out = h->red + size_t(4) * nb;
+  CK(launch_residual(h->dp, h->f[h->cur], h->usnap, h->d_area, have, kResidualChunk, h->red, nullptr, 1,
+                     out, h->stream));
+  double tot[4];
+  CK(cudaMemcpyAsync(tot, out, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  int rc = check_status(h);
+  if (rc != FVDBM_OK) return rc;
+  const long long K = h->steps_done - h->snap_step;
+  *mass = tot[2];
+  if (tot[3] > 0.0)
+    *res_u = std::nan("");
+  else if (!have || K <= 0)
+    *res_u = HUGE_VAL;
+  else
+    *res_u = std::sqrt(tot[0]) / (double(K) * double(h->params.delta_t) * std::max(std::sqrt(tot[1]), 1e-30));
+  h->snap_step = h->steps_done;
+  return FVDBM_OK;
+}
+
+int fvdbm_run_to_steady(void* handle, double threshold, int32_t check_every, int64_t max_steps,
+                        int64_t* steps_taken, double* res_u) {
+  if (!handle || !steps_taken || !res_u) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (check_every <= 0 || max_steps < 0) return fail(h, FVDBM_EINVAL, "check_every <= 0 or max_steps < 0");
+  double r = HUGE_VAL, m = 0.0;
+  int rc;
+  if (h->snap_step != h->steps_done && (rc = fvdbm_residual(h, &r, &m)) != FVDBM_OK) return rc;
+  r = HUGE_VAL;
+  int64_t taken = 0;
+  while (taken < max_steps) {
+    const int n = int(std::min<int64_t>(check_every, max_steps - taken));
+    if ((rc = fvdbm_step(h, n)) != FVDBM_OK) return rc;
+    taken += n;
+    if ((rc = fvdbm_residual(h, &r, &m)) != FVDBM_OK) return rc;
+    if (std::isnan(r) || r < threshold) break;
+  }
+  *steps_taken = taken;
+  *res_u = r;
   return FVDBM_OK;
 }
 

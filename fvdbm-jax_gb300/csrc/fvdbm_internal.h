@@ -103,6 +103,7 @@ struct HostPlan {
   std::vector<float> nd_w, nd_sumw;
 
   std::vector<float> inv_area;  // [Np] when fv
+  std::vector<float> area;      // [Np] when the mesh gives cell areas (mass weights)
 
   // tile tables (valid when tile_ok)
   bool tile_ok = false;
@@ -227,6 +228,13 @@ cudaError_t launch_gather(const DevPlan& p, const float* fin, const float* flux,
                           cudaStream_t s);
 cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
                           cudaStream_t s);
+// FP64 residual / mass partial sums (monitor.cu): one block per chunk of
+// cells, then one block per segment of chunks (seg == nullptr: all chunks,
+// one segment).  out[4*s..] = {sum |du|^2, sum |u_prev|^2, sum rho*A, bad cells}.
+int residual_chunks(int N, int chunk);
+cudaError_t launch_residual(const DevPlan& p, const float* f, float* usnap, const float* area,
+                            bool have_snap, int chunk, double* part, const int* seg, int nseg,
+                            double* out, cudaStream_t s);
 // Counts the float32 dividends x (all 2^32 bit patterns) for which the
 // known-divisor division differs from x / y, and the lowest such bit pattern;
 // *bad must be zeroed and *example set to 0xFFFFFFFF.

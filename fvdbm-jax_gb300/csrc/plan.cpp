@@ -584,6 +584,10 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
     hp.inv_area.assign(hp.Np, 0.0f);
     for (int i = 0; i < N; ++i) hp.inv_area[i] = m.cell_inv_area[hp.cell_old[i]];
   }
+  if (m.cell_area) {
+    hp.area.assign(hp.Np, 0.0f);
+    for (int i = 0; i < N; ++i) hp.area[i] = m.cell_area[hp.cell_old[i]];
+  }
 
   // algorithmic bytes of one step: pdf read+write, cell->face slots, face
   // geometry (2 slot ints + n + L, + 2 distances for Lax-Wendroff) and the

@@ -119,6 +119,8 @@ class Environment:
         xy = getattr(c, "centroids", None)
         a["xy"] = None if xy is None else np.ascontiguousarray(xy, F32)
         a["ia"] = None
+        area = getattr(c, "areas", None)
+        a["area"] = None if area is None else np.ascontiguousarray(np.asarray(area, F32).reshape(-1), F32)
         if self.finite_volume:
             area = getattr(c, "areas", None)
             if area is None:
@@ -131,7 +133,7 @@ class Environment:
                         nat.iptr(a["cfi"]), nat.iptr(a["cfs"]), nat.iptr(a["fc"]), nat.fptr(a["fd"]),
                         nat.iptr(a["fn_"]), nat.fptr(a["fnrm"]), nat.fptr(a["fL"]), nat.fptr(a["scale"]),
                         nat.iptr(a["nt"]), nat.iptr(a["nc"]), nat.fptr(a["nd"]), nat.fptr(a["xy"]),
-                        nat.fptr(a["ia"]))
+                        nat.fptr(a["ia"]), nat.fptr(a["area"]))
         params = nat.Params(nat.FVDBM_UPWIND if f.flux_scheme == "upwind" else nat.FVDBM_LAX_WENDROFF,
                             variant, float(dyn.inv_tau), float(dyn.dt32), float(dyn.c2),
                             float(dyn.c4x2), float(dyn.c2x2), _ORDER[order], _KERNEL[self.kernel],
@@ -173,6 +175,29 @@ class Environment:
             self._steps += int(n_steps)
             self._version += 1
         return self
+
+    def residual(self):
+        """(res_u, mass) of the current state in double: the velocity change
+        since the previous call per unit time, relative to the previous
+        velocity norm, and sum(rho * area) (``fvdbm_residual``)."""
+        if self._h is None:
+            self.init()
+        r, m = C.c_double(), C.c_double()
+        nat.check(nat.lib().fvdbm_residual(self._h, C.byref(r), C.byref(m)), self._h)
+        return r.value, m.value
+
+    def run_to_steady(self, threshold: float = 1e-6, check_every: int = 100, max_steps: int = 1_000_000):
+        """Step until the residual falls below ``threshold`` (checked every
+        ``check_every`` steps) or ``max_steps``; returns (steps, res_u)."""
+        if self._h is None:
+            self.init()
+        n, r = C.c_int64(), C.c_double()
+        nat.check(nat.lib().fvdbm_run_to_steady(self._h, float(threshold), int(check_every), int(max_steps),
+                                                C.byref(n), C.byref(r)), self._h)
+        if n.value:
+            self._steps += n.value
+            self._version += 1
+        return n.value, r.value
 
     def sync(self):
         if self._h is not None:

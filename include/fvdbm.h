@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FVDBM_ABI_VERSION 1
+#define FVDBM_ABI_VERSION 2
 
 #define FVDBM_OK 0
 #define FVDBM_EINVAL (-1)  /* invalid argument or inconsistent mesh */
@@ -86,6 +86,8 @@ typedef struct fvdbm_mesh {
   const float *cell_xy;              /* [N][2] cell centroids for MORTON, or NULL */
   const float *cell_inv_area;        /* [N] 1/area to scale the flux sum, or NULL
                                         (NULL = the reference's update, no area) */
+  const float *cell_area;            /* [N] cell areas weighting the mass of
+                                        fvdbm_residual, or NULL (weight 1) */
 } fvdbm_mesh_t;
 
 /* Step parameters, all float32 as the reference evaluates them
@@ -179,6 +181,25 @@ const char *fvdbm_last_error(void *handle);
 int fvdbm_destroy(void *handle);
 
 int fvdbm_abi_version(void);
+
+/* Convergence monitor (the reference has none; it steps a fixed count).
+ * Velocity residual and total mass of the current cell pdfs, in double:
+ *   res_u = ||u - u_prev||_2 / (K * delta_t * max(||u_prev||_2, 1e-30))
+ *   mass  = sum_i rho_i * area_i     (area 1 when the mesh gave no cell_area)
+ * u, rho are the float32 macros of each cell (src/dynamics.py:35-47); u_prev
+ * is the velocity at the previous fvdbm_residual call, K the steps taken
+ * since then.  res_u is +inf on the first call, after fvdbm_set_state of the
+ * cell pdfs, or when no step was taken since the previous call; NaN when a
+ * cell's rho or u is not finite.  Sums are formed in a fixed order: results
+ * are bitwise reproducible.  Synchronises the handle's stream. */
+int fvdbm_residual(void *handle, double *res_u, double *mass);
+
+/* Steps in chunks of check_every until res_u < threshold (or is NaN), or
+ * max_steps steps were taken.  steps_taken and res_u receive the outcome
+ * (res_u of the last check).  The first residual snapshot is taken before
+ * the first chunk when none is current. */
+int fvdbm_run_to_steady(void *handle, double threshold, int32_t check_every, int64_t max_steps,
+                        int64_t *steps_taken, double *res_u);
 
 /* Largest padded face count (faces rounded up to a multiple of 128, at least
  * 128) that fvdbm_step_static_scratch takes: its face-flux scratch is a fixed

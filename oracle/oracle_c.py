@@ -3,7 +3,9 @@ the C restatement of the reference step (see that file's header).  Only
 ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs use it.
 
 ``step(geo, state, inv_tau, dt, n_steps)`` takes the same ``geo``/``state``
-dicts as ``oracle_np`` and returns the same result dict.
+dicts as ``oracle_np`` and returns the same result dict.  ``step64(geo,
+state, tau, dt, n_steps)`` runs the same statements in float64 (the
+``-DORACLE_F64`` build) and returns float64 arrays.
 """
 from __future__ import annotations
 
@@ -16,11 +18,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "fvdbm_oracle.c")
 LIB = os.path.join(HERE, "_build", "libfvdbm_oracle.so")
+LIB64 = os.path.join(HERE, "_build", "libfvdbm_oracle64.so")
 CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
 
 F32 = np.float32
 _i32p = C.POINTER(C.c_int32)
 _f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
 
 
 class OracleMesh(C.Structure):
@@ -34,18 +38,29 @@ class OracleMesh(C.Structure):
                 ("c4x2", C.c_float), ("c2x2", C.c_float)]
 
 
-def build(force: bool = False) -> str:
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        cmd = ["gcc", *CFLAGS, SRC, "-o", LIB + ".tmp"]
+class OracleMesh64(C.Structure):
+    _fields_ = OracleMesh._fields_[:-5] + [("inv_tau", C.c_double), ("dt", C.c_double), ("c2", C.c_double),
+                                           ("c4x2", C.c_double), ("c2x2", C.c_double)]
+
+
+def _build_one(out, defines, force):
+    if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(SRC):
+        cmd = ["gcc", *CFLAGS, *defines, SRC, "-o", out + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stderr}")
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+        os.replace(out + ".tmp", out)
+    return out
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    _build_one(LIB64, ["-DORACLE_F64"], force)
+    return _build_one(LIB, [], force)
 
 
 _L = None
+_L64 = None
 
 
 def lib():
@@ -57,6 +72,17 @@ def lib():
         L.oracle_max_threads.restype = C.c_int
         _L = L
     return _L
+
+
+def lib64():
+    global _L64
+    if _L64 is None:
+        build()
+        L = C.CDLL(LIB64)
+        L.oracle_step_f64.argtypes = [C.POINTER(OracleMesh64), _f64p, _f64p, _f64p, _f64p, C.c_int, C.c_int,
+                                      _f64p, _f64p, _f64p, _f64p]
+        _L64 = L
+    return _L64
 
 
 def max_threads() -> int:
@@ -87,8 +113,11 @@ def face_scale(geo):
 class Prepared:
     """Contiguous arrays and the C struct for one mesh (kept alive together)."""
 
-    def __init__(self, geo, inv_tau, dt, inv_area=None):
+    def __init__(self, geo, inv_tau, dt, inv_area=None, f64=False):
         from oracle_np import C2, C4X2, C2X2
+        if f64:  # inv_tau is 1/tau in double; lattice constants of C = 1/sqrt(3) in double
+            c = 1.0 / np.sqrt(3.0)
+            C2, C4X2, C2X2 = c * c, 2.0 * ((c * c) * (c * c)), 2.0 * (c * c)
         self.a = {
             "fi": np.ascontiguousarray(geo["face_indices"], np.int32),
             "fs": np.ascontiguousarray(geo["face_signs"], np.int32),
@@ -108,7 +137,7 @@ class Prepared:
         N, F, P = a["fi"].shape[0], a["fc"].shape[0], a["nt"].shape[0]
         self.N, self.F, self.P = N, F, P
         scheme = {"upwind": 0, "lax_wendroff": 1}[geo["scheme"]]
-        self.m = OracleMesh(N, F, P, a["fi"].shape[1], a["nc"].shape[1],
+        self.m = (OracleMesh64 if f64 else OracleMesh)(N, F, P, a["fi"].shape[1], a["nc"].shape[1],
                             _p(a["fi"], _i32p), _p(a["fs"], _i32p), _p(a["fc"], _i32p), _p(a["fd"], _f32p),
                             _p(a["fnd"], _i32p), _p(a["fn"], _f32p), _p(a["fL"], _f32p),
                             _p(a["scale"], _f32p), _p(a["nt"], _i32p), _p(a["nc"], _i32p),
@@ -128,6 +157,26 @@ def step(geo, state, inv_tau, dt, n_steps: int = 1, threads: int = 0, inv_area=N
     rc = lib().oracle_step(C.byref(pr.m), _p(pdf, _f32p), _p(npdf, _f32p), _p(nrho, _f32p), _p(nvel, _f32p),
                            int(n_steps), int(threads), _p(rho, _f32p), _p(vel, _f32p), _p(eq, _f32p),
                            _p(fl, _f32p))
+    if rc != 0:
+        raise MemoryError("oracle scratch allocation failed")
+    return {"cells_pdf": pdf, "cells_rho": rho.reshape(N, 1), "cells_vel": vel, "cells_pdf_eq": eq,
+            "faces_pdf": fl, "nodes_pdf": npdf, "nodes_rho": nrho.reshape(P, 1), "nodes_vel": nvel}
+
+
+def step64(geo, state, tau, dt, n_steps: int = 1, threads: int = 0, inv_area=None, prepared=None):
+    """``step`` in float64: 1/tau and dt taken in double, state promoted."""
+    pr = prepared or Prepared(geo, 1.0 / float(tau), float(dt), inv_area, f64=True)
+    N, F, P = pr.N, pr.F, pr.P
+    D = np.float64
+    pdf = np.array(state["cells_pdf"], D, order="C", copy=True)
+    npdf = np.array(state["nodes_pdf"], D, order="C", copy=True)
+    nrho = np.array(np.asarray(state["nodes_rho"]).reshape(-1), D, copy=True)
+    nvel = np.array(state["nodes_vel"], D, order="C", copy=True)
+    rho, vel = np.empty(N, D), np.empty((N, 2), D)
+    eq, fl = np.empty((N, 9), D), np.empty((F, 9), D)
+    rc = lib64().oracle_step_f64(C.byref(pr.m), _p(pdf, _f64p), _p(npdf, _f64p), _p(nrho, _f64p),
+                                 _p(nvel, _f64p), int(n_steps), int(threads), _p(rho, _f64p), _p(vel, _f64p),
+                                 _p(eq, _f64p), _p(fl, _f64p))
     if rc != 0:
         raise MemoryError("oracle scratch allocation failed")
     return {"cells_pdf": pdf, "cells_rho": rho.reshape(N, 1), "cells_vel": vel, "cells_pdf_eq": eq,
