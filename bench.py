@@ -8,8 +8,9 @@ float32.  Inputs are synthetic (seeded mesh generator; Triangle is not
 available).
 
 A bench step is one FVDBM time step over the whole mesh.  Between timed steps
-L2 is flushed by writing a buffer of 2x L2 size on the step's stream, so each
-timed step reads its inputs from HBM.  Each step is bracketed by CUDA events
+L2 is flushed by writing a buffer of 2x L2 size on the step's stream and then
+reading it back (so the lines left in L2 are clean and the timed step pays no
+write-back of the flush data): each timed step reads its inputs from HBM.  Each step is bracketed by CUDA events
 on the library's stream; the cell kernel (the dominant one) is timed on its
 own for the roofline.
 
@@ -266,6 +267,12 @@ def run_gb300(args):
     N = info["n_cells"]
     stream = torch.cuda.ExternalStream(env.stream_ptr, device=f"cuda:{local}")
     flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    flush_sum = torch.zeros((), dtype=torch.int64, device=f"cuda:{local}")
+
+    def flush_l2(k):
+        # write 2x L2, then read it: L2 holds only clean, unrelated lines
+        flush.fill_(k & 0xFF)
+        flush_sum.add_(flush.view(torch.int64).sum())
 
     # warm-up (graph replay, as a long run would)
     env.step(max(args.warmup, 3))
@@ -284,7 +291,7 @@ def run_gb300(args):
     t_wall = time.perf_counter()
     for k in range(K):
         with torch.cuda.stream(stream):
-            flush.fill_(k & 0xFF)
+            flush_l2(k)
         ev[k][0].record(stream)
         nat.check(L.fvdbm_step(h, 1), h)
         ev[k][1].record(stream)
@@ -302,7 +309,7 @@ def run_gb300(args):
     evp = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(Kp)]
     for k in range(Kp):
         with torch.cuda.stream(stream):
-            flush.fill_(k & 0xFF)
+            flush_l2(k)
         evp[k][0].record(stream)
         nat.check(L.fvdbm_step_phase(h, 1), h)
         evp[k][1].record(stream)
@@ -372,7 +379,7 @@ def run_gb300(args):
 
     if rank == 0:
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                     "l2": "flushed between timed steps (2x L2 write on the step's stream)",
+                     "l2": "flushed between timed steps (2x L2 written, then read back, on the step's stream)",
                      "kernel": {1: "staged", 2: "fused", 3: "tile", 4: "tile_split", 5: "one"}[info["kernel"]],
                      "launches_per_step": info["launches_per_step"],
                      "ctas_per_sm": info["ctas_per_sm"]})

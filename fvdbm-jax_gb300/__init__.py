@@ -14,6 +14,7 @@ from .dynamics import D2Q9
 from .containers import Cells, Faces, Nodes
 from .mesher import Mesher
 from .environment import Environment
+from .batch import Batch
 from . import meshgen
 
-__all__ = ["D2Q9", "Cells", "Faces", "Nodes", "Mesher", "Environment", "meshgen"]
+__all__ = ["D2Q9", "Cells", "Faces", "Nodes", "Mesher", "Environment", "Batch", "meshgen"]

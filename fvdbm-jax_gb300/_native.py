@@ -17,6 +17,7 @@ FVDBM_UPWIND, FVDBM_LAX_WENDROFF = 0, 1
 VARIANT_NONE, VARIANT_FACE_SCALE, VARIANT_FACE_Q_SCALE = 0, 1, 2
 ORDER_NONE, ORDER_RCM, ORDER_MORTON = 0, 1, 2
 KERNEL_AUTO, KERNEL_STAGED, KERNEL_FUSED, KERNEL_TILE, KERNEL_TILE_SPLIT, KERNEL_ONE = 0, 1, 2, 3, 4, 5
+KERNEL_BATCH = 6
 
 _i32p = C.POINTER(C.c_int32)
 _f32p = C.POINTER(C.c_float)
@@ -57,7 +58,9 @@ _LIB = None
 EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", "fvdbm_get_cells", "fvdbm_get_nodes",
            "fvdbm_get_face_fluxes", "fvdbm_sync", "fvdbm_stream", "fvdbm_get_info",
            "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check",
-           "fvdbm_step_static_scratch", "fvdbm_residual", "fvdbm_run_to_steady"]
+           "fvdbm_step_static_scratch", "fvdbm_residual", "fvdbm_run_to_steady",
+           "fvdbm_batch_create", "fvdbm_batch_config", "fvdbm_batch_residual", "fvdbm_batch_set_active",
+           "fvdbm_batch_run_to_steady"]
 
 
 def lib_path() -> str:
@@ -80,6 +83,12 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_step_phase.argtypes = [vp, C.c_int32]
     L.fvdbm_step_static_scratch.argtypes = [vp, C.c_int32]
     L.fvdbm_residual.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    _f64p, _i64p = C.POINTER(C.c_double), C.POINTER(C.c_int64)
+    L.fvdbm_batch_create.argtypes = [C.POINTER(Mesh), C.POINTER(Params), C.c_int32, C.POINTER(vp)]
+    L.fvdbm_batch_config.argtypes = [vp, C.c_int32, C.c_int32]
+    L.fvdbm_batch_residual.argtypes = [vp, _f64p, _f64p]
+    L.fvdbm_batch_set_active.argtypes = [vp, _i32p]
+    L.fvdbm_batch_run_to_steady.argtypes = [vp, C.c_double, C.c_int32, _i64p, _i64p, _f64p, _i32p]
     L.fvdbm_run_to_steady.argtypes = [vp, C.c_double, C.c_int32, C.c_int64, C.POINTER(C.c_int64),
                                       C.POINTER(C.c_double)]
     L.fvdbm_get_cells.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]

@@ -37,6 +37,17 @@ struct Handle {
   bool fused = false;
   bool tile = false;
   bool one = false;  // node and cell blocks in one launch
+  // packed batch of independent cases (fvdbm_batch_create)
+  bool batch = false;
+  int batch_block = 256, batch_waves = 1;
+  std::vector<int> active;          // per case, host copy of case_active
+  std::vector<long long> case_steps; // steps each case has taken
+  int* d_active = nullptr;
+  int* d_chunk_start = nullptr;  // residual chunks inside the case ranges
+  int* d_case_chunk = nullptr;   // first chunk of each case
+  int n_chunks = 0;
+  std::vector<float> case_dt_host;
+  double* bred = nullptr;  // batch residual partials, then 4 totals per case
   int* status = nullptr;
   std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -166,7 +177,11 @@ int enqueue_steps(Handle* h, int n) {
   for (int s = 0; s < n; ++s) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
-    if (h->one) {
+    if (h->batch) {
+      CK(launch_nodes(h->dp, fin, h->stream, /*pdl=*/s > 0));
+      CK(launch_fused_batch(h->dp, fin, fout, h->stream, /*pdl=*/h->dp.NB > 0 || s > 0, h->batch_block,
+                            h->batch_waves));
+    } else if (h->one) {
       CK(launch_step(h->dp, fin, fout, h->stream, /*pdl=*/s > 0));
     } else if (h->tile) {
       if (!h->dp.tile_nodes) CK(launch_nodes(h->dp, fin, h->stream));
@@ -251,7 +266,8 @@ int fvdbm_destroy(void* handle) {
   return FVDBM_OK;
 }
 
-int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** handle) {
+static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, const BatchSegs* segs,
+                       const float* case_inv_tau, const float* case_dt, void** handle) {
   auto create_fail = [&](Handle* h, int code) {
     {
       std::lock_guard<std::mutex> lk(g_err_mu);
@@ -265,7 +281,7 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   Handle* h = new Handle();
   h->params = *params;
   h->device = params->device;
-  std::string why = build_plan(mesh, params, h->hp);
+  std::string why = build_plan(mesh, params, h->hp, segs);
   if (!why.empty()) {
     h->err = why;
     return create_fail(h, FVDBM_EINVAL);
@@ -306,6 +322,15 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
     return create_fail(h, FVDBM_EINVAL);
   }
   h->one = one_possible && params->kernel == FVDBM_KERNEL_ONE;
+  if (segs) {
+    if (!(hp.fusable && hp.K == 3)) {
+      h->err = "a batch needs triangles (3 face slots per cell), every cell face slot naming a face of "
+               "that cell, and no per-q flux scale";
+      return create_fail(h, FVDBM_EINVAL);
+    }
+    h->batch = true;
+    h->fused = h->tile = h->one = false;
+  }
   h->dp.tile_nodes = (params->kernel == FVDBM_KERNEL_TILE) ? 1 : 0;
   p.N = hp.N;
   p.Np = hp.Np;
@@ -353,7 +378,7 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
   UP(cf_face, hp.cf_face);
   UP(cf_sign, hp.cf_sign);
   p.hrows = hp.hrows;
-  if (h->fused) {
+  if (h->fused || h->batch) {
     UP(hf, hp.hf);
     UP(gh_a, hp.gh_a);
     UP(gh_b, hp.gh_b);
@@ -418,8 +443,30 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
     if ((rc = dalloc<float>(h, &h->f[b], size_t(Q) * hp.Np)) != FVDBM_OK) return create_fail(h, rc);
     CR(cudaMemsetAsync(h->f[b], 0, size_t(Q) * hp.Np * 4, h->stream));
   }
-  if (!h->fused)
+  if (!h->fused && !h->batch)
     if ((rc = dalloc<float>(h, &h->flux, size_t(Q) * hp.Fp)) != FVDBM_OK) return create_fail(h, rc);
+  if (h->batch) {
+    const std::vector<float> it(case_inv_tau, case_inv_tau + hp.S), dt(case_dt, case_dt + hp.S);
+    h->case_dt_host = dt;
+    h->active.assign(hp.S, 1);
+    h->case_steps.assign(hp.S, 0);
+    UP(cell_case, hp.cell_case);
+    UP(case_inv_tau, it);
+    UP(case_dt, dt);
+    if ((rc = dalloc(h, &h->d_active, h->active.size(), &h->active)) != FVDBM_OK) return create_fail(h, rc);
+    p.case_active = h->d_active;
+    // residual chunks of at most kResidualChunk cells inside each case
+    std::vector<int> cs, cc;
+    for (int s = 0; s < hp.S; ++s) {
+      cc.push_back(int(cs.size()));
+      for (int c = hp.case_cell[s]; c < hp.case_cell[s + 1]; c += kResidualChunk) cs.push_back(c);
+    }
+    cc.push_back(int(cs.size()));
+    h->n_chunks = int(cs.size());
+    cs.push_back(hp.N);
+    if ((rc = dalloc(h, &h->d_chunk_start, cs.size(), &cs)) != FVDBM_OK) return create_fail(h, rc);
+    if ((rc = dalloc(h, &h->d_case_chunk, cc.size(), &cc)) != FVDBM_OK) return create_fail(h, rc);
+  }
   if ((rc = dalloc<float>(h, &h->stage, size_t(Q) * std::max(hp.N, hp.F))) != FVDBM_OK)
     return create_fail(h, rc);
   if ((rc = dalloc(h, &h->d_cell_new, hp.cell_new.size(), &hp.cell_new)) != FVDBM_OK)
@@ -449,6 +496,164 @@ int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** 
 #undef UP
 }
 
+int fvdbm_create(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, void** handle) {
+  return create_impl(mesh, params, nullptr, nullptr, nullptr, handle);
+}
+
+int fvdbm_batch_create(const fvdbm_mesh_t* meshes, const fvdbm_params_t* params, int32_t n_cases,
+                       void** handle) {
+  auto bad = [](const std::string& why) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = why;
+    return FVDBM_EINVAL;
+  };
+  if (!meshes || !params || !handle || n_cases <= 0) return bad("invalid arguments");
+  *handle = nullptr;
+  for (int s = 1; s < n_cases; ++s) {
+    const fvdbm_params_t &a = params[0], &b = params[s];
+    if (a.flux_scheme != b.flux_scheme || a.variant != b.variant || a.c2 != b.c2 || a.c4x2 != b.c4x2 ||
+        a.c2x2 != b.c2x2 || a.ordering != b.ordering || a.device != b.device)
+      return bad("batch case " + std::to_string(s) + ": parameters other than inv_tau and delta_t differ");
+  }
+  if (params[0].variant != FVDBM_VARIANT_NONE) return bad("a batch takes no flux-scale variant");
+  UnionMesh u;
+  std::string why = build_union(meshes, n_cases, u);
+  if (!why.empty()) return bad(why);
+  std::vector<float> it(n_cases), dt(n_cases);
+  for (int s = 0; s < n_cases; ++s) {
+    it[s] = params[s].inv_tau;
+    dt[s] = params[s].delta_t;
+  }
+  fvdbm_params_t p0 = params[0];
+  p0.kernel = FVDBM_KERNEL_FUSED;
+  return create_impl(&u.mesh, &p0, &u.segs, it.data(), dt.data(), handle);
+}
+
+int fvdbm_batch_config(void* handle, int32_t block, int32_t prefetch_waves) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+  if ((block != 128 && block != 256) || prefetch_waves < 0 || prefetch_waves > 8)
+    return fail(h, FVDBM_EINVAL, "block must be 128 or 256 and prefetch_waves 0..8");
+  if (block == h->batch_block && prefetch_waves == h->batch_waves) return FVDBM_OK;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  for (auto& g : h->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  h->batch_block = block;
+  h->batch_waves = prefetch_waves;
+  return FVDBM_OK;
+}
+
+int fvdbm_batch_residual(void* handle, double* res_u, double* mass) {
+  if (!handle || !res_u || !mass) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+  const HostPlan& hp = h->hp;
+  const int S = hp.S;
+  CK(cudaSetDevice(h->device));
+  int rc;
+  if (!h->usnap && (rc = dalloc<float>(h, &h->usnap, size_t(2) * hp.Np)) != FVDBM_OK) return rc;
+  if (!h->bred && (rc = dalloc<double>(h, &h->bred, size_t(4) * (h->n_chunks + S))) != FVDBM_OK) return rc;
+  const bool have = h->snap_step >= 0;
+  double* out = h->bred + size_t(4) * h->n_chunks;
+  CK(launch_residual(h->dp, h->f[h->cur], h->usnap, h->d_area, have, kResidualChunk, h->d_chunk_start,
+                     h->n_chunks, h->bred, h->d_case_chunk, S, out, h->stream));
+  std::vector<double> tot(size_t(4) * S);
+  CK(cudaMemcpyAsync(tot.data(), out, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if ((rc = check_status(h)) != FVDBM_OK) return rc;
+  const long long K = h->steps_done - h->snap_step;
+  for (int s = 0; s < S; ++s) {
+    const double* t = &tot[size_t(4) * s];
+    mass[s] = t[2];
+    if (t[3] > 0.0)
+      res_u[s] = std::nan("");
+    else if (!have || K <= 0)
+      res_u[s] = HUGE_VAL;
+    else
+      res_u[s] = std::sqrt(t[0]) / (double(K) * double(h->case_dt_host[s]) * std::max(std::sqrt(t[1]), 1e-30));
+  }
+  h->snap_step = h->steps_done;
+  return FVDBM_OK;
+}
+
+int fvdbm_batch_set_active(void* handle, const int32_t* active) {
+  if (!handle || !active) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  bool changed = false;
+  for (int s = 0; s < hp.S; ++s) {
+    const int a = active[s] ? 1 : 0;
+    if (a == h->active[s]) continue;
+    changed = true;
+    // both buffers must hold the final state of a retired case
+    if (!a) CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
+    h->active[s] = a;
+  }
+  if (changed) {
+    CK(cudaMemcpyAsync(h->d_active, h->active.data(), h->active.size() * sizeof(int), cudaMemcpyHostToDevice,
+                       h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  return FVDBM_OK;
+}
+
+int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_every, const int64_t* max_steps,
+                              int64_t* steps, double* res_u, int32_t* status) {
+  if (!handle || !max_steps || !steps || !res_u || !status) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+  if (check_every <= 0) return fail(h, FVDBM_EINVAL, "check_every <= 0");
+  const int S = h->hp.S;
+  std::vector<int32_t> act(S);
+  std::vector<double> r(S, HUGE_VAL), m(S);
+  for (int s = 0; s < S; ++s) {
+    if (max_steps[s] < 0) return fail(h, FVDBM_EINVAL, "max_steps < 0");
+    steps[s] = 0;
+    res_u[s] = HUGE_VAL;
+    status[s] = 0;
+    act[s] = max_steps[s] > 0;
+  }
+  int rc = fvdbm_batch_set_active(h, act.data());
+  if (rc != FVDBM_OK) return rc;
+  if ((rc = fvdbm_batch_residual(h, r.data(), m.data())) != FVDBM_OK) return rc;  // snapshot
+  for (;;) {
+    int64_t n = check_every;
+    bool any = false;
+    for (int s = 0; s < S; ++s)
+      if (act[s]) {
+        any = true;
+        n = std::min<int64_t>(n, max_steps[s] - steps[s]);
+      }
+    if (!any) break;
+    if ((rc = fvdbm_step(h, int32_t(n))) != FVDBM_OK) return rc;
+    for (int s = 0; s < S; ++s)
+      if (act[s]) steps[s] += n;
+    if ((rc = fvdbm_batch_residual(h, r.data(), m.data())) != FVDBM_OK) return rc;
+    for (int s = 0; s < S; ++s) {
+      if (!act[s]) continue;
+      res_u[s] = r[s];
+      if (std::isnan(r[s])) {
+        status[s] = 2;
+        act[s] = 0;
+      } else if (r[s] < threshold) {
+        status[s] = 1;
+        act[s] = 0;
+      } else if (steps[s] >= max_steps[s]) {
+        act[s] = 0;
+      }
+    }
+    if ((rc = fvdbm_batch_set_active(h, act.data())) != FVDBM_OK) return rc;
+  }
+  return FVDBM_OK;
+}
+
 int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, const float* node_rho,
                     const float* node_vel) {
   if (!handle) return FVDBM_EINVAL;
@@ -459,6 +664,10 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
     CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(Q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
     CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream));
     if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
+    // a retired batch case keeps its state in both buffers
+    for (size_t s = 0; s < h->active.size(); ++s)
+      if (!h->active[s])
+        CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
     h->snap_step = -1;
   }
   if (node_pdf || node_rho || node_vel) {
@@ -489,6 +698,8 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   int rc = enqueue_steps(h, n);
   if (rc != FVDBM_OK) return rc;
   h->steps_done += n_steps;
+  for (size_t s = 0; s < h->active.size(); ++s)
+    if (h->active[s]) h->case_steps[s] += n_steps;
   return FVDBM_OK;
 }
 
@@ -524,7 +735,9 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
     else if (!h->one && (!h->tile || !h->dp.tile_nodes))
       CK(launch_nodes(h->dp, fin, h->stream));
   } else if (phase == 2) {
-    if (h->one) {
+    if (h->batch) {
+      CK(launch_fused_batch(h->dp, fin, fout, h->stream, false, h->batch_block, h->batch_waves));
+    } else if (h->one) {
       CK(launch_step(h->dp, fin, fout, h->stream, false));
     } else if (h->tile) {
       CK(launch_tile(h->dp, fin, fout, h->stream));
@@ -655,8 +868,8 @@ int fvdbm_residual(void* handle, double* res_u, double* mass) {
   }
   const bool have = h->snap_step >= 0;
   double* out = h->red + size_t(4) * nb;
-  CK(launch_residual(h->dp, h->f[h->cur], h->usnap, h->d_area, have, kResidualChunk, h->red, nullptr, 1,
-                     out, h->stream));
+  CK(launch_residual(h->dp, h->f[h->cur], h->usnap, h->d_area, have, kResidualChunk, nullptr, 0, h->red,
+                     nullptr, 1, out, h->stream));
   double tot[4];
   CK(cudaMemcpyAsync(tot, out, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -707,11 +920,11 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->one ? FVDBM_KERNEL_ONE
+  info->kernel = h->batch ? FVDBM_KERNEL_BATCH : h->one ? FVDBM_KERNEL_ONE
                          : h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
                                    : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
   const int node_launch = (hp.Mc > 0 && !h->one && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
-  info->launches_per_step = node_launch + (h->one || h->tile ? 1 : (h->fused ? 1 : 2));
+  info->launches_per_step = node_launch + (h->one || h->tile || h->batch ? 1 : (h->fused ? 1 : 2));
   info->padded_cells = hp.Np;
   info->ctas_per_sm = h->tile ? tile_ctas_per_sm(h->dp) : 0;
   info->const_division = (h->dp.d_c2.ok && h->dp.d_c4x2.ok && h->dp.d_c2x2.ok) ? 1 : 0;

@@ -8,6 +8,8 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/fvdbm.h"
+
 namespace fvdbm {
 
 constexpr int Q = 9;
@@ -117,12 +119,37 @@ struct HostPlan {
 
   bool finite_n = true;
   double bytes_per_step = 0.0;
+
+  // packed batch of independent cases (S > 0): case s owns device cells
+  // [case_cell[s], case_cell[s+1]); cell_case[i] is the case of device cell i
+  int S = 0;
+  std::vector<int32_t> case_cell;
+  std::vector<int32_t> cell_case;  // [Np]
 };
 
-struct MeshIn;  // fvdbm_mesh_t
+// Segments of a union mesh: case s owns cells [cell_ptr[s], cell_ptr[s+1]),
+// faces [face_ptr[s], ..) and nodes [node_ptr[s], ..).  A padded -1 node
+// stencil entry of a case wraps to that case's last cell.
+struct BatchSegs {
+  int S;
+  const int32_t* cell_ptr;
+  const int32_t* face_ptr;
+  const int32_t* node_ptr;
+};
 
 // Build the plan; returns an empty string on success, else the reason.
-std::string build_plan(const void* mesh, const void* params, HostPlan& hp);
+std::string build_plan(const void* mesh, const void* params, HostPlan& hp,
+                       const BatchSegs* segs = nullptr);
+
+// The union of S cases' meshes (batch.cpp); `mesh` points into the vectors.
+struct UnionMesh {
+  int K = 0, Kn = 0;
+  std::vector<int32_t> cfi, cfs, fc, fnd, nt, nc, cell_ptr, face_ptr, node_ptr;
+  std::vector<float> fd, fn, fL, nd, xy, ia, area;
+  fvdbm_mesh_t mesh{};
+  BatchSegs segs{};
+};
+std::string build_union(const fvdbm_mesh_t* meshes, int S, UnionMesh& u);
 
 // Division by a divisor known in advance: y and zr = RN(1/y).  ok says the
 // three-operation form was verified against IEEE division for every float32
@@ -202,6 +229,11 @@ struct DevPlan {
   int* step_ctr;  // single-launch step: ticket, node blocks published, blocks finished
   const unsigned char* cblk_ghost;  // per 256-cell block: has a ghost face
   const int* sched;                 // single-launch tickets: cell block >= 0, node block -(b+1)
+  // packed batch: per-cell case, per-case 1/tau, dt and active flag
+  const int* cell_case;
+  const float* case_inv_tau;
+  const float* case_dt;
+  const int* case_active;
 };
 
 constexpr int STATUS_WAIT_TIMEOUT = 1;
@@ -231,10 +263,17 @@ cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* v
 // FP64 residual / mass partial sums (monitor.cu): one block per chunk of
 // cells, then one block per segment of chunks (seg == nullptr: all chunks,
 // one segment).  out[4*s..] = {sum |du|^2, sum |u_prev|^2, sum rho*A, bad cells}.
+// chunk_start (nullable): chunk b covers cells [chunk_start[b], chunk_start[b+1]).
 int residual_chunks(int N, int chunk);
 cudaError_t launch_residual(const DevPlan& p, const float* f, float* usnap, const float* area,
-                            bool have_snap, int chunk, double* part, const int* seg, int nseg,
-                            double* out, cudaStream_t s);
+                            bool have_snap, int chunk, const int* chunk_start, int nchunks,
+                            double* part, const int* seg, int nseg, double* out, cudaStream_t s);
+// packed batch: the fused cell kernel with per-case 1/tau, dt and retirement
+// (threads per block 128 or 256; L2 prefetch distance in waves)
+cudaError_t launch_fused_batch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl,
+                               int block, int prefetch_waves);
+// copy device cells [c0, c1) of an AoSoA pdf buffer
+cudaError_t launch_copy_cells(const float* src, float* dst, int c0, int c1, cudaStream_t s);
 // Counts the float32 dividends x (all 2^32 bit patterns) for which the
 // known-divisor division differs from x / y, and the lowest such bit pattern;
 // *bad must be zeroed and *example set to 0xFFFFFFFF.

@@ -5,6 +5,7 @@
 // Layout: cell pdfs are AoSoA [Np/32][9][32] float32 in device (renumbered)
 // cell order; the fused kernel's per-cell face slots are AoSoA
 // [Np/32][hrows][32]; node state is SoA [9][Mp].
+#include <algorithm>
 #include <utility>
 
 #include "fvdbm_math.cuh"
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(256) k_stencil_macros(DevPlan p, const float* 
 template <int SCHEME, int VARIANT, bool FIRST, bool GHOST_CG>
 __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin,
                                            const unsigned* __restrict__ hb, int k, int code, float nx,
-                                           float ny, float Ls, const float f[Q], float acc[Q]) {
+                                           float ny, float Ls, float dt, const float f[Q], float acc[Q]) {
   const HfRows HR{3, SCHEME, VARIANT};
   const int other = code >> HF_SHIFT;
   const bool slot1 = (code & HF_SLOT1) != 0;
@@ -250,7 +251,7 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
   float w[Q];
   if (SCHEME == 1)
     lw_interp(v, __uint_as_float(__ldg(hb + HR.r(k) * 32)), __uint_as_float(__ldg(hb + HR.d2(k) * 32)),
-              p.dt, p.finite_n != 0, w);
+              dt, p.finite_n != 0, w);
   const float scale = (VARIANT == 1) ? __uint_as_float(__ldg(hb + HR.sc(k) * 32)) : 1.0f;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -274,21 +275,20 @@ __device__ __forceinline__ void prefetch_l2(const void* ptr, uint32_t bytes) {
 
 // One cell of the fused update.  GHOST_CG: read node pdfs through L2 (they
 // were written earlier in the same launch).  RECORD: node-stencil cells also
-// record the macros of their new pdfs.
+// record the macros of their new pdfs.  inv_tau and dt are the cell's case's.
 template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG, bool RECORD = false>
-__device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __restrict__ fin,
-                                           float* __restrict__ fout, int i, const int code[3],
-                                           const float nx[3], const float ny[3], const float Ls[3],
-                                           const unsigned* __restrict__ hb) {
-  float f[Q];
-  load_cell(fin, i, f);
+__device__ __forceinline__ void fused_cell_f(const DevPlan& p, const float* __restrict__ fin,
+                                             float* __restrict__ fout, int i, const float f[Q],
+                                             const int code[3], const float nx[3], const float ny[3],
+                                             const float Ls[3], const unsigned* __restrict__ hb,
+                                             float inv_tau, float dt) {
+  float acc[Q];
+  fused_face<SCHEME, VARIANT, true, GHOST_CG>(p, fin, hb, 0, code[0], nx[0], ny[0], Ls[0], dt, f, acc);
+  fused_face<SCHEME, VARIANT, false, GHOST_CG>(p, fin, hb, 1, code[1], nx[1], ny[1], Ls[1], dt, f, acc);
+  fused_face<SCHEME, VARIANT, false, GHOST_CG>(p, fin, hb, 2, code[2], nx[2], ny[2], Ls[2], dt, f, acc);
   float rho, ux, uy, eq[Q];
   macros(f, rho, ux, uy);
   feq9(rho, ux, uy, p, eq);
-  float acc[Q];
-  fused_face<SCHEME, VARIANT, true, GHOST_CG>(p, fin, hb, 0, code[0], nx[0], ny[0], Ls[0], f, acc);
-  fused_face<SCHEME, VARIANT, false, GHOST_CG>(p, fin, hb, 1, code[1], nx[1], ny[1], Ls[1], f, acc);
-  fused_face<SCHEME, VARIANT, false, GHOST_CG>(p, fin, hb, 2, code[2], nx[2], ny[2], Ls[2], f, acc);
   if (FV) {
     const float ia = __ldg(p.inv_area + i);
 #pragma unroll
@@ -298,10 +298,20 @@ __device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __rest
   float fn[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    fn[q] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+    fn[q] = f[q] + dt * (inv_tau * (eq[q] - f[q]) - acc[q]);
     o[q * 32] = fn[q];
   }
   if (RECORD && i >= p.stencil_start) record_stencil(p, i, fn);
+}
+
+template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG, bool RECORD = false>
+__device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __restrict__ fin,
+                                           float* __restrict__ fout, int i, const int code[3],
+                                           const float nx[3], const float ny[3], const float Ls[3],
+                                           const unsigned* __restrict__ hb) {
+  float f[Q];
+  load_cell(fin, i, f);
+  fused_cell_f<SCHEME, VARIANT, FV, GHOST_CG, RECORD>(p, fin, fout, i, f, code, nx, ny, Ls, hb, p.inv_tau, p.dt);
 }
 
 template <int SCHEME, int VARIANT>
@@ -327,16 +337,47 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
   // the block about one wave ahead streams into L2 while this one computes
   const int ahead = blockIdx.x + prefetch_blocks;
   const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead < int(gridDim.x);
-  if (do_prefetch) prefetch_l2(p.hf + size_t(ahead) * 256 * HROWS, 256 * HROWS * sizeof(unsigned));
+  // cells [ahead*256, min(+256, Np)): whole 32-cell groups, a multiple of 16 bytes
+  const int pf_cells = do_prefetch ? min(256, p.Np - ahead * 256) : 0;
+  if (pf_cells > 0) prefetch_l2(p.hf + size_t(ahead) * 256 * HROWS, pf_cells * HROWS * sizeof(unsigned));
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned* hb;
   int code[3];
   float nx[3], ny[3], Ls[3];
   load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
   grid_dep_wait();  // fin and the node pdfs come from the previous kernels
-  if (do_prefetch) prefetch_l2(fin + size_t(ahead) * 256 * Q, 256 * Q * sizeof(float));
+  if (pf_cells > 0) prefetch_l2(fin + size_t(ahead) * 256 * Q, pf_cells * Q * sizeof(float));
   if (i >= p.N) return;
   fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
+}
+
+// Packed batch of independent cases: the same cell update with the cell's
+// case's 1/tau and dt; cells of retired cases are neither read nor written
+// (both pdf buffers hold their final state).  Block size 128 or 256; the
+// block `prefetch_blocks` ahead streams into L2.
+template <int SCHEME, int VARIANT, bool FV>
+__global__ void __launch_bounds__(256) k_fused_batch(DevPlan p, const float* __restrict__ fin,
+                                                     float* __restrict__ fout, int prefetch_blocks) {
+  constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+  grid_dep_launch();
+  const int T = blockDim.x;
+  const int i = blockIdx.x * T + threadIdx.x;
+  const int cs = __ldg(p.cell_case + min(i, p.Np - 1));
+  const int ahead = blockIdx.x + prefetch_blocks;
+  const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead < int(gridDim.x);
+  const int pf_cells = do_prefetch ? min(T, p.Np - ahead * T) : 0;
+  if (pf_cells > 0) prefetch_l2(p.hf + size_t(ahead) * T * HROWS, pf_cells * HROWS * sizeof(unsigned));
+  const unsigned* hb;
+  int code[3];
+  float nx[3], ny[3], Ls[3];
+  load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
+  const float inv_tau = __ldg(p.case_inv_tau + cs), dt = __ldg(p.case_dt + cs);
+  grid_dep_wait();  // fin, the node pdfs and the active flags come from earlier work
+  if (pf_cells > 0) prefetch_l2(fin + size_t(ahead) * T * Q, pf_cells * Q * sizeof(float));
+  if (i >= p.N || !p.case_active[cs]) return;
+  float f[Q];
+  load_cell(fin, i, f);
+  fused_cell_f<SCHEME, VARIANT, FV, false, false>(p, fin, fout, i, f, code, nx, ny, Ls, hb, inv_tau, dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -648,6 +689,43 @@ static cudaError_t fused_dispatch(const DevPlan& p, const float* fin, float* fou
   const int pf = fused_prefetch_blocks();
   if (p.fv) return launch_ex(k_fused<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, pf);
   return launch_ex(k_fused<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, pf);
+}
+
+template <int S, int V>
+static cudaError_t fused_batch_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
+                                        bool pdl, int block, int waves) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int g = blocks(p.N, block);
+  const int pf = waves * sms * (2048 / block) / 2;  // about `waves` waves at half occupancy
+  if (p.fv) return launch_ex(k_fused_batch<S, V, true>, g, block, 0, s, pdl, p, fin, fout, pf);
+  return launch_ex(k_fused_batch<S, V, false>, g, block, 0, s, pdl, p, fin, fout, pf);
+}
+
+cudaError_t launch_fused_batch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl,
+                               int block, int prefetch_waves) {
+  if (p.N == 0) return cudaSuccess;
+  if (p.K != 3 || (block != 128 && block != 256) || prefetch_waves < 0) return cudaErrorInvalidValue;
+  if (p.scheme == 0 && p.variant == 0) return fused_batch_dispatch<0, 0>(p, fin, fout, s, pdl, block, prefetch_waves);
+  if (p.scheme == 1 && p.variant == 0) return fused_batch_dispatch<1, 0>(p, fin, fout, s, pdl, block, prefetch_waves);
+  if (p.scheme == 0 && p.variant == 1) return fused_batch_dispatch<0, 1>(p, fin, fout, s, pdl, block, prefetch_waves);
+  if (p.scheme == 1 && p.variant == 1) return fused_batch_dispatch<1, 1>(p, fin, fout, s, pdl, block, prefetch_waves);
+  return cudaErrorInvalidValue;
+}
+
+__global__ void k_copy_cells(const float* __restrict__ src, float* __restrict__ dst, int c0, int c1) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = c0 + t / Q, q = t % Q;
+  if (c >= c1) return;
+  const size_t o = cell_base(c, Q) + size_t(q) * 32;
+  dst[o] = src[o];
+}
+
+cudaError_t launch_copy_cells(const float* src, float* dst, int c0, int c1, cudaStream_t s) {
+  if (c1 <= c0) return cudaSuccess;
+  k_copy_cells<<<blocks(int64_t(c1 - c0) * Q, 256), 256, 0, s>>>(src, dst, c0, c1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl) {

@@ -130,7 +130,30 @@ std::vector<int32_t> rcm_order(int N, int F, const int32_t* fc) {
 
 }  // namespace
 
-std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
+// Order of the cells of one case (segment [a, b) of a union mesh whose faces
+// [fa, fb) belong to it): Morton when centroids are given, else RCM.
+std::vector<int32_t> segment_order(const fvdbm_mesh_t& m, int ordering, int a, int b, int fa, int fb) {
+  const int n = b - a;
+  std::vector<int32_t> loc;
+  if (ordering == FVDBM_ORDER_MORTON && m.cell_xy) {
+    loc = morton_order(m.cell_xy + 2 * int64_t(a), n);
+  } else if (ordering == FVDBM_ORDER_RCM) {
+    std::vector<int32_t> fc(2 * size_t(fb - fa));
+    for (int f = fa; f < fb; ++f)
+      for (int k = 0; k < 2; ++k) {
+        const int32_t c = m.face_cells[2 * f + k];
+        fc[2 * size_t(f - fa) + k] = c < 0 ? -1 : c - a;
+      }
+    loc = rcm_order(n, fb - fa, fc.data());
+  } else {
+    loc.resize(n);
+    std::iota(loc.begin(), loc.end(), 0);
+  }
+  for (auto& c : loc) c += a;
+  return loc;
+}
+
+std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, const BatchSegs* segs) {
   const fvdbm_mesh_t& m = *static_cast<const fvdbm_mesh_t*>(mesh_v);
   const fvdbm_params_t& pr = *static_cast<const fvdbm_params_t*>(params_v);
   std::ostringstream err;
@@ -195,9 +218,52 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       }
   }
 
+  // ---- packed batch: every reference stays inside its own case
+  std::vector<int32_t> node_seg;
+  if (segs) {
+    const int S = segs->S;
+    if (S <= 0 || segs->cell_ptr[0] != 0 || segs->cell_ptr[S] != N || segs->face_ptr[0] != 0 ||
+        segs->face_ptr[S] != F || segs->node_ptr[0] != 0 || segs->node_ptr[S] != P)
+      return "batch segments do not cover the union mesh";
+    node_seg.assign(P, 0);
+    for (int s = 0; s < S; ++s) {
+      const int c0 = segs->cell_ptr[s], c1 = segs->cell_ptr[s + 1];
+      const int f0 = segs->face_ptr[s], f1 = segs->face_ptr[s + 1];
+      const int n0 = segs->node_ptr[s], n1 = segs->node_ptr[s + 1];
+      if (c1 <= c0 || f1 < f0 || n1 < n0) return "batch case " + std::to_string(s) + " is empty or inverted";
+      auto inside = [](int32_t x, int lo, int hi) { return x >= lo && x < hi; };
+      for (int c = c0; c < c1; ++c)
+        for (int k = 0; k < K; ++k)
+          if (!inside(m.cell_face_indices[int64_t(c) * K + k], f0, f1))
+            return "batch case " + std::to_string(s) + ": a cell names a face of another case";
+      for (int f = f0; f < f1; ++f)
+        for (int k = 0; k < 2; ++k) {
+          const int32_t c = m.face_cells[2 * f + k], nd = m.face_nodes[2 * f + k];
+          if ((c != -1 && !inside(c, c0, c1)) || !inside(nd, n0, n1))
+            return "batch case " + std::to_string(s) + ": a face names a cell or node of another case";
+        }
+      for (int p_ = n0; p_ < n1; ++p_) {
+        node_seg[p_] = s;
+        for (int k = 0; k < Kn; ++k) {
+          const int32_t c = m.node_cells[int64_t(p_) * Kn + k];
+          if (c != -1 && !inside(c, c0, c1))
+            return "batch case " + std::to_string(s) + ": a node names a cell of another case";
+        }
+      }
+    }
+  }
+
   // ---- cell order
   hp.ordering = pr.ordering;
-  if (pr.ordering == FVDBM_ORDER_MORTON && m.cell_xy && N > 0)
+  if (segs && N > 0) {
+    hp.cell_old.clear();
+    for (int s = 0; s < segs->S; ++s) {
+      auto o = segment_order(m, pr.ordering, segs->cell_ptr[s], segs->cell_ptr[s + 1], segs->face_ptr[s],
+                             segs->face_ptr[s + 1]);
+      hp.cell_old.insert(hp.cell_old.end(), o.begin(), o.end());
+    }
+    if (pr.ordering == FVDBM_ORDER_MORTON && !m.cell_xy) hp.ordering = FVDBM_ORDER_NONE;
+  } else if (pr.ordering == FVDBM_ORDER_MORTON && m.cell_xy && N > 0)
     hp.cell_old = morton_order(m.cell_xy, N);
   else if (pr.ordering == FVDBM_ORDER_RCM && N > 0)
     hp.cell_old = rcm_order(N, F, m.face_cells);
@@ -212,7 +278,7 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
   // single-launch step form the tail of its grid.  (Not for the in-tile node
   // kernel, whose tiles must stay compact.)
   hp.stencil_start = N;
-  if (N > 0 && Kn > 0 && pr.kernel != FVDBM_KERNEL_TILE) {
+  if (N > 0 && Kn > 0 && pr.kernel != FVDBM_KERNEL_TILE && !segs) {
     std::vector<char> member(N, 0);
     for (int p_ = 0; p_ < P; ++p_) {
       if (m.node_type[p_] == 0) continue;
@@ -290,12 +356,13 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
       float w = 1.0f / dist;
       if (w < 0.0f) w = 0.0f;
       sumw = (k == 0) ? w : sumw + w;
-      if (c == -1 && w == 0.0f) {
+      if (c == -1 && w == 0.0f && !segs) {
         hp.nd_npad[d]++;
         continue;
       }
       if (N == 0) return "nodes reference cells but there are none";
-      uint32_t code = uint32_t(cnew_wrap(c));
+      // a batch case's -1 entries wrap to that case's last cell
+      uint32_t code = uint32_t(segs && c == -1 ? hp.cell_new[segs->cell_ptr[node_seg[p] + 1] - 1] : cnew_wrap(c));
       if (c == -1) code |= ND_NEQ_ZERO;
       hp.nd_cell.push_back(code);
       hp.nd_w.push_back(w);
@@ -587,6 +654,15 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp) {
   if (m.cell_area) {
     hp.area.assign(hp.Np, 0.0f);
     for (int i = 0; i < N; ++i) hp.area[i] = m.cell_area[hp.cell_old[i]];
+  }
+  if (segs) {
+    // cases keep their ranges: the order is a permutation within each case
+    hp.S = segs->S;
+    hp.case_cell.assign(segs->cell_ptr, segs->cell_ptr + segs->S + 1);
+    hp.cell_case.assign(hp.Np, 0);
+    for (int s = 0; s < segs->S; ++s)
+      for (int i = segs->cell_ptr[s]; i < segs->cell_ptr[s + 1]; ++i) hp.cell_case[i] = s;
+    for (int i = N; i < hp.Np; ++i) hp.cell_case[i] = segs->S - 1;
   }
 
   // algorithmic bytes of one step: pdf read+write, cell->face slots, face

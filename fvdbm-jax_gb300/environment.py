@@ -55,6 +55,59 @@ def _face_scale(faces):
     return nat.VARIANT_NONE, None
 
 
+def pack(c, f, n, *, ordering="auto", kernel="auto", device=0, finite_volume=False):
+    """The C-ABI mesh and parameter structs of one case (``fvdbm_mesh_t``,
+    ``fvdbm_params_t``), the arrays they point into (keep them alive), the
+    sizes (N, F, P) and the case's D2Q9 dynamics."""
+    if f.flux_scheme not in ("upwind", "lax_wendroff"):
+        raise ValueError(f"Unknown flux scheme: {f.flux_scheme}")
+    dyn = c.dynamics
+    if not isinstance(dyn, D2Q9):
+        dyn = D2Q9(dyn.tau, dyn.delta_t)
+    a = {
+        "cfi": np.ascontiguousarray(c.face_indices, I32),
+        "cfs": np.ascontiguousarray(c.face_normals, I32),
+        "fc": np.ascontiguousarray(f.stencil_cells_index, I32),
+        "fd": np.ascontiguousarray(f.stencil_dists, F32),
+        "fn_": np.ascontiguousarray(f.nodes_index, I32),
+        "fnrm": np.ascontiguousarray(f.n, F32),
+        "fL": np.ascontiguousarray(np.asarray(f.L, F32).reshape(-1)),
+        "nt": np.ascontiguousarray(np.asarray(n.type, I32).reshape(-1)),
+        "nc": np.ascontiguousarray(n.cells_index, I32),
+        "nd": np.ascontiguousarray(n.cell_dists, F32),
+    }
+    N, F, P = a["cfi"].shape[0], a["fc"].shape[0], a["nt"].shape[0]
+    if a["nc"].shape[0] != P or a["nd"].shape != a["nc"].shape:
+        raise ValueError("Nodes.cells_index / cell_dists shapes disagree")
+    if a["cfs"].shape != a["cfi"].shape:
+        raise ValueError("Cells.face_indices / face_normals shapes disagree")
+    variant, scale = _face_scale(f)
+    a["scale"] = scale
+    xy = getattr(c, "centroids", None)
+    a["xy"] = None if xy is None else np.ascontiguousarray(xy, F32)
+    a["ia"] = None
+    area = getattr(c, "areas", None)
+    a["area"] = None if area is None else np.ascontiguousarray(np.asarray(area, F32).reshape(-1), F32)
+    if finite_volume:
+        area = getattr(c, "areas", None)
+        if area is None:
+            raise ValueError("finite_volume=True needs cell areas (cells.areas)")
+        a["ia"] = np.ascontiguousarray(F32(1) / np.asarray(area, F32).reshape(-1), F32)
+    order = ordering
+    if order == "auto":
+        order = "morton" if a["xy"] is not None else "rcm"
+    mesh = nat.Mesh(N, F, P, a["cfi"].shape[1] if N else 0, a["nc"].shape[1] if P else 0,
+                    nat.iptr(a["cfi"]), nat.iptr(a["cfs"]), nat.iptr(a["fc"]), nat.fptr(a["fd"]),
+                    nat.iptr(a["fn_"]), nat.fptr(a["fnrm"]), nat.fptr(a["fL"]), nat.fptr(a["scale"]),
+                    nat.iptr(a["nt"]), nat.iptr(a["nc"]), nat.fptr(a["nd"]), nat.fptr(a["xy"]),
+                    nat.fptr(a["ia"]), nat.fptr(a["area"]))
+    params = nat.Params(nat.FVDBM_UPWIND if f.flux_scheme == "upwind" else nat.FVDBM_LAX_WENDROFF,
+                        variant, float(dyn.inv_tau), float(dyn.dt32), float(dyn.c2),
+                        float(dyn.c4x2), float(dyn.c2x2), _ORDER[order], _KERNEL[kernel],
+                        int(device))
+    return mesh, params, a, (N, F, P), dyn
+
+
 class Environment:
     """GB300 FVDBM environment (reference ``Environment``)."""
 
@@ -91,53 +144,9 @@ class Environment:
         c, f, n = self.cells, self.faces, self.nodes
         for cont in (c, f, n):
             cont.init()
-        if f.flux_scheme not in ("upwind", "lax_wendroff"):
-            raise ValueError(f"Unknown flux scheme: {f.flux_scheme}")
-        dyn = c.dynamics
-        if not isinstance(dyn, D2Q9):
-            dyn = D2Q9(dyn.tau, dyn.delta_t)
+        mesh, params, keep, (N, F, P), dyn = pack(c, f, n, ordering=self.ordering, kernel=self.kernel,
+                                                  device=self.device, finite_volume=self.finite_volume)
         L = nat.lib()
-        a = {
-            "cfi": np.ascontiguousarray(c.face_indices, I32),
-            "cfs": np.ascontiguousarray(c.face_normals, I32),
-            "fc": np.ascontiguousarray(f.stencil_cells_index, I32),
-            "fd": np.ascontiguousarray(f.stencil_dists, F32),
-            "fn_": np.ascontiguousarray(f.nodes_index, I32),
-            "fnrm": np.ascontiguousarray(f.n, F32),
-            "fL": np.ascontiguousarray(np.asarray(f.L, F32).reshape(-1)),
-            "nt": np.ascontiguousarray(np.asarray(n.type, I32).reshape(-1)),
-            "nc": np.ascontiguousarray(n.cells_index, I32),
-            "nd": np.ascontiguousarray(n.cell_dists, F32),
-        }
-        N, F, P = a["cfi"].shape[0], a["fc"].shape[0], a["nt"].shape[0]
-        if a["nc"].shape[0] != P or a["nd"].shape != a["nc"].shape:
-            raise ValueError("Nodes.cells_index / cell_dists shapes disagree")
-        if a["cfs"].shape != a["cfi"].shape:
-            raise ValueError("Cells.face_indices / face_normals shapes disagree")
-        variant, scale = _face_scale(f)
-        a["scale"] = scale
-        xy = getattr(c, "centroids", None)
-        a["xy"] = None if xy is None else np.ascontiguousarray(xy, F32)
-        a["ia"] = None
-        area = getattr(c, "areas", None)
-        a["area"] = None if area is None else np.ascontiguousarray(np.asarray(area, F32).reshape(-1), F32)
-        if self.finite_volume:
-            area = getattr(c, "areas", None)
-            if area is None:
-                raise ValueError("finite_volume=True needs cell areas (cells.areas)")
-            a["ia"] = np.ascontiguousarray(F32(1) / np.asarray(area, F32).reshape(-1), F32)
-        order = self.ordering
-        if order == "auto":
-            order = "morton" if a["xy"] is not None else "rcm"
-        mesh = nat.Mesh(N, F, P, a["cfi"].shape[1] if N else 0, a["nc"].shape[1] if P else 0,
-                        nat.iptr(a["cfi"]), nat.iptr(a["cfs"]), nat.iptr(a["fc"]), nat.fptr(a["fd"]),
-                        nat.iptr(a["fn_"]), nat.fptr(a["fnrm"]), nat.fptr(a["fL"]), nat.fptr(a["scale"]),
-                        nat.iptr(a["nt"]), nat.iptr(a["nc"]), nat.fptr(a["nd"]), nat.fptr(a["xy"]),
-                        nat.fptr(a["ia"]), nat.fptr(a["area"]))
-        params = nat.Params(nat.FVDBM_UPWIND if f.flux_scheme == "upwind" else nat.FVDBM_LAX_WENDROFF,
-                            variant, float(dyn.inv_tau), float(dyn.dt32), float(dyn.c2),
-                            float(dyn.c4x2), float(dyn.c2x2), _ORDER[order], _KERNEL[self.kernel],
-                            int(self.device))
         self.close()
         h = C.c_void_p()
         rc = L.fvdbm_create(C.byref(mesh), C.byref(params), C.byref(h))

@@ -64,6 +64,7 @@ extern "C" {
 #define FVDBM_KERNEL_TILE 3       /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
 #define FVDBM_KERNEL_TILE_SPLIT 4 /* node BC kernel + persistent tile kernel (2 kernels) */
 #define FVDBM_KERNEL_ONE 5        /* node and cell blocks in one launch (1 kernel) */
+#define FVDBM_KERNEL_BATCH 6      /* (reported by fvdbm_get_info) packed batch: node BC + fused cell kernel */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {
@@ -200,6 +201,39 @@ int fvdbm_residual(void *handle, double *res_u, double *mass);
  * the first chunk when none is current. */
 int fvdbm_run_to_steady(void *handle, double threshold, int32_t check_every, int64_t max_steps,
                         int64_t *steps_taken, double *res_u);
+
+/* ---- Packed batch (no counterpart in the reference, which steps one
+ * Environment at a time).  n_cases independent cases in one handle: their
+ * meshes are joined into one device mesh (cells of a case stay contiguous,
+ * ordered within the case), so each step is one node launch and one cell
+ * launch for all cases, with each case's own 1/tau and delta_t.  Every case
+ * evolves bit for bit as it would in its own handle.  Cases that converge
+ * retire: their cells are no longer read or written.  Needs triangles (3
+ * face slots per cell) and no flux-scale variant; params[s] may differ only in
+ * inv_tau and delta_t.  fvdbm_step / fvdbm_get_cells / fvdbm_get_nodes /
+ * fvdbm_residual act on the union (cells, nodes in case order). */
+int fvdbm_batch_create(const fvdbm_mesh_t *meshes, const fvdbm_params_t *params, int32_t n_cases,
+                       void **handle);
+
+/* Launch shape of the batch cell kernel: threads per block (128 or 256) and
+ * the L2 prefetch distance in waves (0 = none).  The autotuner sets these. */
+int fvdbm_batch_config(void *handle, int32_t block, int32_t prefetch_waves);
+
+/* Per-case residual and mass (as fvdbm_residual, per case).  [n_cases]. */
+int fvdbm_batch_residual(void *handle, double *res_u, double *mass);
+
+/* Mark cases active (1) or retired (0).  A retired case's cells keep their
+ * current state in both buffers and are skipped by the step.  [n_cases]. */
+int fvdbm_batch_set_active(void *handle, const int32_t *active);
+
+/* Steps every active case, checking the residuals every check_every steps;
+ * a case retires when its residual falls below threshold (status 1), turns
+ * NaN (status 2) or when it has taken max_steps[s] steps (status 0).
+ * Returns when no case is active.  steps [n_cases] = steps each case took,
+ * res_u = its last residual, status as above.  Arrays are [n_cases]. */
+int fvdbm_batch_run_to_steady(void *handle, double threshold, int32_t check_every,
+                              const int64_t *max_steps, int64_t *steps, double *res_u,
+                              int32_t *status);
 
 /* Largest padded face count (faces rounded up to a multiple of 128, at least
  * 128) that fvdbm_step_static_scratch takes: its face-flux scratch is a fixed
