@@ -47,6 +47,9 @@ struct Handle {
   int* d_case_chunk = nullptr;   // first chunk of each case
   int n_chunks = 0;
   std::vector<float> case_dt_host;
+  int* d_blk = nullptr;  // active cell blocks of the batch launch
+  std::vector<int> blk_host;
+  bool blk_valid = false;
   double* bred = nullptr;  // batch residual partials, then 4 totals per case
   int* status = nullptr;
   std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
@@ -233,6 +236,34 @@ int get_graph(Handle* h, int parity, cudaGraphExec_t* out) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(h, FVDBM_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e));
   *out = h->graph[parity];
+  return FVDBM_OK;
+}
+
+// Cell blocks (of the batch launch's block size) holding cells of active
+// cases; the launch covers only those.  The grid size changes, so captured
+// graphs are dropped.
+int update_batch_blocks(Handle* h) {
+  const HostPlan& hp = h->hp;
+  const int T = h->batch_block;
+  std::vector<int> list;
+  for (int s = 0; s < hp.S; ++s) {
+    if (!h->active[s]) continue;
+    const int b0 = hp.case_cell[s] / T, b1 = (hp.case_cell[s + 1] - 1) / T;
+    for (int b = std::max(b0, list.empty() ? 0 : list.back() + 1); b <= b1; ++b) list.push_back(b);
+  }
+  if (h->blk_valid && list == h->blk_host) return FVDBM_OK;
+  if (!list.empty())
+    CK(cudaMemcpyAsync(h->d_blk, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->dp.blk_list = h->d_blk;
+  h->dp.n_blk = int(list.size());
+  h->blk_host = list;
+  h->blk_valid = true;
+  for (auto& g : h->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
   return FVDBM_OK;
 }
 
@@ -455,6 +486,8 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     UP(case_dt, dt);
     if ((rc = dalloc(h, &h->d_active, h->active.size(), &h->active)) != FVDBM_OK) return create_fail(h, rc);
     p.case_active = h->d_active;
+    if ((rc = dalloc<int>(h, &h->d_blk, size_t(hp.N + 127) / 128)) != FVDBM_OK) return create_fail(h, rc);
+    if ((rc = update_batch_blocks(h)) != FVDBM_OK) return create_fail(h, rc);
     // residual chunks of at most kResidualChunk cells inside each case
     std::vector<int> cs, cc;
     for (int s = 0; s < hp.S; ++s) {
@@ -545,7 +578,8 @@ int fvdbm_batch_config(void* handle, int32_t block, int32_t prefetch_waves) {
     }
   h->batch_block = block;
   h->batch_waves = prefetch_waves;
-  return FVDBM_OK;
+  h->blk_valid = false;  // rebuild for the new block size
+  return update_batch_blocks(h);
 }
 
 int fvdbm_batch_residual(void* handle, double* res_u, double* mass) {
@@ -600,6 +634,7 @@ int fvdbm_batch_set_active(void* handle, const int32_t* active) {
     CK(cudaMemcpyAsync(h->d_active, h->active.data(), h->active.size() * sizeof(int), cudaMemcpyHostToDevice,
                        h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    return update_batch_blocks(h);
   }
   return FVDBM_OK;
 }

@@ -234,6 +234,10 @@ struct DevPlan {
   const float* case_inv_tau;
   const float* case_dt;
   const int* case_active;
+  // cell blocks of the active cases (block size of the batch launch); all
+  // blocks when null
+  const int* blk_list;
+  int n_blk;
 };
 
 constexpr int STATUS_WAIT_TIMEOUT = 1;

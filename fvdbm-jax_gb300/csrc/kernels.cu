@@ -361,10 +361,12 @@ __global__ void __launch_bounds__(256) k_fused_batch(DevPlan p, const float* __r
   constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
   grid_dep_launch();
   const int T = blockDim.x;
-  const int i = blockIdx.x * T + threadIdx.x;
+  const int blk = p.blk_list ? __ldg(p.blk_list + blockIdx.x) : int(blockIdx.x);
+  const int i = blk * T + threadIdx.x;
   const int cs = __ldg(p.cell_case + min(i, p.Np - 1));
-  const int ahead = blockIdx.x + prefetch_blocks;
-  const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead < int(gridDim.x);
+  const int ahead_idx = blockIdx.x + prefetch_blocks;
+  const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead_idx < int(gridDim.x);
+  const int ahead = do_prefetch ? (p.blk_list ? __ldg(p.blk_list + ahead_idx) : ahead_idx) : 0;
   const int pf_cells = do_prefetch ? min(T, p.Np - ahead * T) : 0;
   if (pf_cells > 0) prefetch_l2(p.hf + size_t(ahead) * T * HROWS, pf_cells * HROWS * sizeof(unsigned));
   const unsigned* hb;
@@ -697,7 +699,8 @@ static cudaError_t fused_batch_dispatch(const DevPlan& p, const float* fin, floa
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int g = blocks(p.N, block);
+  const int g = p.blk_list ? p.n_blk : blocks(p.N, block);
+  if (g == 0) return cudaSuccess;
   const int pf = waves * sms * (2048 / block) / 2;  // about `waves` waves at half occupancy
   if (p.fv) return launch_ex(k_fused_batch<S, V, true>, g, block, 0, s, pdl, p, fin, fout, pf);
   return launch_ex(k_fused_batch<S, V, false>, g, block, 0, s, pdl, p, fin, fout, pf);

@@ -209,13 +209,15 @@ def porous_obstacles(n_obstacles: int = 400, mu: float = float(np.log(0.012)), s
 
 
 def porous(n_obstacles: int = 400, n_target: int = 1_000_000, porosity: float = 0.70,
-           mu: float = float(np.log(0.012)), sigma: float = 0.3, seed: int = 0) -> RawMesh:
+           mu: float = float(np.log(0.012)), sigma: float = 0.3, seed: int = 0,
+           gap_cells: float = 2.5) -> RawMesh:
     """Unit square holding ``n_obstacles`` circular obstacles at the given
     porosity, meshed to about ``n_target`` triangles.  Inlet is the left side
-    (marker 4), outlet the right side (marker 2)."""
+    (marker 4), outlet the right side (marker 2).  Obstacles keep
+    ``gap_cells`` mesh spacings clear of each other and of the sides."""
     rng = np.random.default_rng(seed + 1)
     h = float(np.sqrt(4.0 * porosity / (np.sqrt(3.0) * n_target)))
-    circles = porous_obstacles(n_obstacles, mu, sigma, porosity, gap=2.5 * h, seed=seed)
+    circles = porous_obstacles(n_obstacles, mu, sigma, porosity, gap=gap_cells * h, seed=seed)
     m = _delaunay_domain(1.0, 1.0, circles, h, rng)
     solid = float(np.sum(np.pi * circles[:, 2] ** 2))
     m.info = {"kind": "porous", "n_obstacles": n_obstacles, "porosity": 1.0 - solid,
