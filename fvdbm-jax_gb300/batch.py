@@ -118,6 +118,19 @@ class Batch:
                                                  m.ctypes.data_as(C.POINTER(C.c_double))), self._h)
         return r, m
 
+    def set_cells_eq(self, rho, vel):
+        """Every cell's pdf = feq(rho, u) (union arrays rho [N], vel [N,2])."""
+        r = np.ascontiguousarray(np.asarray(rho, F32).reshape(-1))
+        v = np.ascontiguousarray(np.asarray(vel, F32).reshape(-1, 2))
+        nat.check(nat.lib().fvdbm_set_cells_eq(self._h, nat.fptr(r), nat.fptr(v)), self._h)
+
+    def set_case_pdf(self, s: int, pdf):
+        """Replace case s's cell pdfs (the other cases keep their state)."""
+        st = self.state()
+        c0, c1 = int(self.cell_ptr[s]), int(self.cell_ptr[s + 1])
+        st["pdf"][c0:c1] = np.asarray(pdf, F32).reshape(c1 - c0, 9)
+        self._set_state(st["pdf"], None, None, None)
+
     def set_active(self, active):
         a = np.ascontiguousarray(np.asarray(active, np.int32).reshape(self.n_cases))
         nat.check(nat.lib().fvdbm_batch_set_active(self._h, nat.iptr(a)), self._h)

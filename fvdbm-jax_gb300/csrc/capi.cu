@@ -715,6 +715,25 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
   return FVDBM_OK;
 }
 
+int fvdbm_set_cells_eq(void* handle, const float* rho, const float* vel) {
+  if (!handle || !rho || !vel) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  const HostPlan& hp = h->hp;
+  CK(cudaSetDevice(h->device));
+  if (hp.N == 0) return FVDBM_OK;
+  // stage: rho [N] then vel [N][2] (the staging buffer holds 9 max(N, F) floats)
+  CK(cudaMemcpyAsync(h->stage, rho, size_t(hp.N) * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->stage + hp.N, vel, size_t(2) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(launch_cells_eq(h->dp, h->stage, h->stage + hp.N, h->d_cell_new, h->f[h->cur], h->stream));
+  if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
+  for (size_t s = 0; s < h->active.size(); ++s)
+    if (!h->active[s])
+      CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
+  h->snap_step = -1;
+  CK(cudaStreamSynchronize(h->stream));
+  return FVDBM_OK;
+}
+
 int fvdbm_step(void* handle, int32_t n_steps) {
   if (!handle) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);

@@ -276,6 +276,9 @@ cudaError_t launch_residual(const DevPlan& p, const float* f, float* usnap, cons
 // (threads per block 128 or 256; L2 prefetch distance in waves)
 cudaError_t launch_fused_batch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl,
                                int block, int prefetch_waves);
+// cell pdfs = feq(rho, vel) from reference-order device arrays
+cudaError_t launch_cells_eq(const DevPlan& p, const float* rho, const float* vel, const int* cell_new, float* f,
+                            cudaStream_t s);
 // copy device cells [c0, c1) of an AoSoA pdf buffer
 cudaError_t launch_copy_cells(const float* src, float* dst, int c0, int c1, cudaStream_t s);
 // Counts the float32 dividends x (all 2^32 bit patterns) for which the

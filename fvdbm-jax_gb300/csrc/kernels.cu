@@ -725,6 +725,26 @@ __global__ void k_copy_cells(const float* __restrict__ src, float* __restrict__ 
   dst[o] = src[o];
 }
 
+// Cell pdfs = feq(rho, u) (src/dynamics.py:70-74) from reference-order
+// rho [N] and vel [N][2].
+__global__ void k_cells_eq(DevPlan p, const float* __restrict__ rho, const float* __restrict__ vel,
+                           const int* __restrict__ cell_new, float* __restrict__ f) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= p.N) return;
+  float eq[Q];
+  feq9(rho[c], vel[2 * size_t(c)], vel[2 * size_t(c) + 1], p, eq);
+  float* o = f + cell_base(cell_new[c], Q);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) o[q * 32] = eq[q];
+}
+
+cudaError_t launch_cells_eq(const DevPlan& p, const float* rho, const float* vel, const int* cell_new, float* f,
+                            cudaStream_t s) {
+  if (p.N == 0) return cudaSuccess;
+  k_cells_eq<<<blocks(p.N, 256), 256, 0, s>>>(p, rho, vel, cell_new, f);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_copy_cells(const float* src, float* dst, int c0, int c1, cudaStream_t s) {
   if (c1 <= c0) return cudaSuccess;
   k_copy_cells<<<blocks(int64_t(c1 - c0) * Q, 256), 256, 0, s>>>(src, dst, c0, c1);

@@ -1,0 +1,391 @@
+"""Learned warm start: a message-passing network over the cells of a mesh
+predicts the steady rho and u of a case from its geometry; the solver starts
+from f = feq(rho, u) instead of the uniform state and still runs to its
+residual threshold, which judges the result.  A case whose residual stalls is
+restarted from the uniform state.
+
+The reference has no counterpart (it always starts from feq(1, 0),
+src/containers.py:24-30).  The network is trained on steady states that the
+solver itself produces (``Batch.run_to_steady``), by the library's own CUDA
+kernels (include/fvdbm_mpnn.h): bfloat16 weights, float32 activations and
+accumulation, Adam on float32 master weights.  PyTorch only provides the
+device memory and the stream.
+
+Network (hidden 64, 4 message-passing layers):
+    h0 = relu(x W0^T + b0)
+    m_l = A h_{l-1};  h_l = h_{l-1} + relu([h_{l-1} | m_l] W_l^T + b_l)
+    y = h_4 W_out^T + b_out
+with A the mean over a cell's neighbours through interior faces.  Per-cell
+features x: centroid (2), distance to the nearest wall, area, inlet and
+outlet density; outputs: (rho - rho_out)/drho, u/drho (drho = rho_in - rho_out),
+each standardised over the training set.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native as nat
+
+HIDDEN, LAYERS, NFEAT, NOUT = 64, 4, 6, 3
+
+
+# ----------------------------------------------------------------------------
+# graph and features
+def cell_graph(faces, n_cells: int):
+    """Row-normalised adjacency through interior faces: CSR (row_ptr, col, wt)
+    of A and of A^T, each row's entries in ascending column order."""
+    import scipy.sparse as sp
+    fc = np.asarray(faces.stencil_cells_index, np.int64)
+    inner = (fc[:, 0] >= 0) & (fc[:, 1] >= 0) & (fc[:, 0] != fc[:, 1])
+    a, b = fc[inner, 0], fc[inner, 1]
+    M = sp.coo_matrix((np.ones(2 * a.size), (np.concatenate([a, b]), np.concatenate([b, a]))),
+                      shape=(n_cells, n_cells)).tocsr()
+    M.data[:] = 1.0
+    M.sum_duplicates()
+    M.data[:] = 1.0
+    deg = np.asarray(M.sum(1)).reshape(-1)
+    A = sp.diags(np.where(deg > 0, 1.0 / np.maximum(deg, 1), 0.0)) @ M
+    A = A.tocsr().astype(np.float32)
+    A.sort_indices()
+    At = A.T.tocsr()
+    At.sort_indices()
+    pack = lambda S: (S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.float32))
+    return pack(A), pack(At)
+
+
+def wall_distance(mesher, faces, nodes):
+    """Distance from each cell centroid to the nearest wall: the midpoints of
+    boundary faces that are not open (both end nodes density nodes)."""
+    from scipy.spatial import cKDTree
+    fc = np.asarray(faces.stencil_cells_index)
+    fn = np.asarray(faces.nodes_index)
+    t = np.asarray(nodes.type).reshape(-1)
+    bnd = (fc[:, 0] < 0) | (fc[:, 1] < 0)
+    open_ = (t[fn[:, 0]] == 2) & (t[fn[:, 1]] == 2)
+    wall = bnd & ~open_
+    mid = np.asarray(mesher.face_centers, np.float64)[wall]
+    cen = np.asarray(mesher.cell_centers, np.float64)
+    if mid.shape[0] == 0:
+        return np.full(cen.shape[0], 1.0)
+    return cKDTree(mid).query(cen)[0]
+
+
+def features(mesher, cells, faces, nodes, rho_in: float, rho_out: float) -> np.ndarray:
+    cen = np.asarray(mesher.cell_centers, np.float64)
+    area = np.asarray(mesher.cell_areas, np.float64).reshape(-1)
+    wd = wall_distance(mesher, faces, nodes)
+    n = cen.shape[0]
+    return np.stack([cen[:, 0], cen[:, 1], wd, area, np.full(n, rho_in), np.full(n, rho_out)], 1).astype(np.float32)
+
+
+def targets(rho, vel, rho_in: float, rho_out: float) -> np.ndarray:
+    d = rho_in - rho_out
+    rho = np.asarray(rho, np.float64).reshape(-1)
+    vel = np.asarray(vel, np.float64).reshape(-1, 2)
+    return np.stack([(rho - rho_out) / d, vel[:, 0] / d, vel[:, 1] / d], 1).astype(np.float32)
+
+
+def untarget(y, rho_in: float, rho_out: float):
+    d = rho_in - rho_out
+    y = np.asarray(y, np.float64)
+    return (rho_out + d * y[:, 0]).astype(np.float32), (d * y[:, 1:3]).astype(np.float32)
+
+
+class Sample:
+    """One case for the network: features, adjacency and (for training) targets."""
+
+    def __init__(self, x, graph, t=None):
+        self.x = np.asarray(x, np.float32)
+        self.A, self.At = graph
+        self.t = None if t is None else np.asarray(t, np.float32)
+        self.n = self.x.shape[0]
+
+
+def _concat(samples):
+    """Block-diagonal union of several samples' graphs."""
+    def cat(k):
+        ptr, col, wt, off_r, off_c = [np.zeros(1, np.int32)], [], [], 0, 0
+        for s in samples:
+            p, c, w = getattr(s, k)
+            ptr.append(p[1:] + off_r)
+            col.append(c + off_c)
+            wt.append(w)
+            off_r += int(p[-1])
+            off_c += s.n
+        return np.concatenate(ptr), np.concatenate(col), np.concatenate(wt)
+    x = np.concatenate([s.x for s in samples])
+    t = None if samples[0].t is None else np.concatenate([s.t for s in samples])
+    return x, cat("A"), cat("At"), t
+
+
+# ----------------------------------------------------------------------------
+class MPNN:
+    """The warm-start network; parameters live on the GPU (float32 master,
+    bfloat16 copy used by the kernels)."""
+
+    def __init__(self, hidden: int = HIDDEN, layers: int = LAYERS, seed: int = 0, device: int = 0):
+        import torch
+        self.hidden, self.layers, self.device = hidden, layers, device
+        self.shapes = [((hidden, NFEAT), (hidden,))] + [((hidden, 2 * hidden), (hidden,))] * layers + \
+                      [((NOUT, hidden), (NOUT,))]
+        self.offs = []
+        o = 0
+        for ws, bs in self.shapes:
+            nw, nb = int(np.prod(ws)), int(np.prod(bs))
+            self.offs.append((o, o + nw, o + nw + nb))
+            o += nw + nb
+        self.size = o
+        rng = np.random.default_rng(seed)
+        host = np.zeros(o, np.float32)
+        for (ws, _), (a, b, c) in zip(self.shapes, self.offs):
+            host[a:b] = (rng.standard_normal(int(np.prod(ws))) * np.sqrt(2.0 / ws[1])).astype(np.float32)
+        self._dev = f"cuda:{device}"
+        self.P = torch.from_numpy(host).to(self._dev)
+        self.Pb = torch.zeros(o, dtype=torch.int16, device=self._dev)
+        self.G = torch.zeros(o, dtype=torch.float32, device=self._dev)
+        self.M = torch.zeros_like(self.G)
+        self.V = torch.zeros_like(self.G)
+        self.step_count = 0
+        self.x_mu = np.zeros(NFEAT, np.float32)
+        self.x_sd = np.ones(NFEAT, np.float32)
+        self.t_mu = np.zeros(NOUT, np.float32)
+        self.t_sd = np.ones(NOUT, np.float32)
+        self._sync_bf16()
+
+    # -- plumbing ------------------------------------------------------------
+    def _stream(self):
+        import torch
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    @staticmethod
+    def _p(t):
+        return 0 if t is None else int(t.data_ptr())
+
+    def _w(self, l, buf=None):
+        """Address of layer l's weights in buf (default: the bfloat16 copy)."""
+        buf = self.Pb if buf is None else buf
+        return self._p(buf) + buf.element_size() * self.offs[l][0]
+
+    def _b(self, l, buf=None):
+        """Address of layer l's bias in buf (default: the float32 master)."""
+        buf = self.P if buf is None else buf
+        return self._p(buf) + buf.element_size() * self.offs[l][1]
+
+    def _sync_bf16(self):
+        nat.check(nat.lib().fvdbm_mp_to_bf16(self._p(self.P), self._p(self.Pb), self.size, self._stream()))
+
+    def get_params(self, rounded: bool = True):
+        """[(W, b)] on the host; W rounded to bfloat16 as the kernels see it."""
+        host = self.P.detach().cpu().numpy()
+        out = []
+        for (ws, bs), (a, b, c) in zip(self.shapes, self.offs):
+            W = host[a:b].reshape(ws)
+            if rounded:
+                u = W.view(np.uint32).astype(np.uint64)
+                W = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32).view(np.float32)
+            out.append((W.copy(), host[b:c].copy()))
+        return out
+
+    def set_params(self, params):
+        import torch
+        host = np.zeros(self.size, np.float32)
+        for (W, bb), (a, b, c) in zip(params, self.offs):
+            host[a:b] = np.asarray(W, np.float32).reshape(-1)
+            host[b:c] = np.asarray(bb, np.float32).reshape(-1)
+        self.P.copy_(torch.from_numpy(host))
+        self._sync_bf16()
+
+    def grads(self):
+        host = self.G.detach().cpu().numpy()
+        return [(host[a:b].reshape(ws).copy(), host[b:c].copy()) for (ws, _), (a, b, c) in zip(self.shapes, self.offs)]
+
+    # -- device batch ---------------------------------------------------------
+    def _upload(self, samples, with_targets: bool):
+        import torch
+        x, A, At, t = _concat(samples)
+        xn = (x - self.x_mu) / self.x_sd
+        d = self._dev
+        g = {"n": x.shape[0], "x": torch.from_numpy(np.ascontiguousarray(xn, np.float32)).to(d),
+             "A": [torch.from_numpy(np.ascontiguousarray(a)).to(d) for a in A],
+             "At": [torch.from_numpy(np.ascontiguousarray(a)).to(d) for a in At]}
+        if with_targets:
+            tn = (t - self.t_mu) / self.t_sd
+            g["t"] = torch.from_numpy(np.ascontiguousarray(tn, np.float32)).to(d)
+        n, H = g["n"], self.hidden
+        g["h"] = [torch.empty((n, H), device=d) for _ in range(self.layers + 1)]
+        g["z"] = [torch.empty((n, H), device=d) for _ in range(self.layers + 1)]
+        g["m"] = [torch.empty((n, H), device=d) for _ in range(self.layers)]
+        g["y"] = torch.empty((n, NOUT), device=d)
+        return g
+
+    def _forward(self, g):
+        L, s, n, H = nat.lib(), self._stream(), g["n"], self.hidden
+        P = self._p
+        nat.check(L.fvdbm_mp_dense_fwd(P(g["x"]), NFEAT, 0, 0, n, self._w(0), self._b(0), H, 1, 0,
+                                       P(g["z"][0]), P(g["h"][0]), s))
+        for l in range(1, self.layers + 1):
+            hp = g["h"][l - 1]
+            nat.check(L.fvdbm_mp_spmm(P(g["A"][0]), P(g["A"][1]), P(g["A"][2]), n, P(hp), H, P(g["m"][l - 1]), 0, s))
+            nat.check(L.fvdbm_mp_dense_fwd(P(hp), H, P(g["m"][l - 1]), H, n, self._w(l), self._b(l), H, 1, P(hp),
+                                           P(g["z"][l]), P(g["h"][l]), s))
+        lo = self.layers + 1
+        nat.check(L.fvdbm_mp_dense_fwd(P(g["h"][-1]), H, 0, 0, n, self._w(lo), self._b(lo), NOUT, 0, 0, 0,
+                                       P(g["y"]), s))
+
+    def _backward(self, g, dy):
+        import torch
+        L, s, n, H = nat.lib(), self._stream(), g["n"], self.hidden
+        P = self._p
+        scratch_n = max(L.fvdbm_mp_wgrad_scratch(n, H, 2 * H), L.fvdbm_mp_wgrad_scratch(n, NOUT, H),
+                        L.fvdbm_mp_wgrad_scratch(n, H, NFEAT))
+        if g.get("wscr") is None or g["wscr"].numel() * 4 < scratch_n:
+            g["wscr"] = torch.empty((scratch_n + 3) // 4, dtype=torch.float32, device=self._dev)
+            g["dh"] = torch.empty((n, H), device=self._dev)
+            g["dz"] = torch.empty((n, H), device=self._dev)
+            g["dm"] = torch.empty((n, H), device=self._dev)
+        ws, wsn = P(g["wscr"]), g["wscr"].numel() * 4
+        lo = self.layers + 1
+        G = self.G
+        nat.check(L.fvdbm_mp_dense_bwd_weight(P(dy), n, NOUT, P(g["h"][-1]), H, 0, 0, self._w(lo, G), self._b(lo, G),
+                                              ws, wsn, s))
+        nat.check(L.fvdbm_mp_dense_bwd_data(P(dy), n, NOUT, self._w(lo), H, 0, P(g["dh"]), 0, 0, s))
+        for l in range(self.layers, 0, -1):
+            nat.check(L.fvdbm_mp_relu_bwd(P(g["dh"]), P(g["z"][l]), P(g["dz"]), n * H, s))
+            nat.check(L.fvdbm_mp_dense_bwd_weight(P(g["dz"]), n, H, P(g["h"][l - 1]), H, P(g["m"][l - 1]), H,
+                                                  self._w(l, G), self._b(l, G), ws, wsn, s))
+            nat.check(L.fvdbm_mp_dense_bwd_data(P(g["dz"]), n, H, self._w(l), H, H, P(g["dh"]), 1, P(g["dm"]), s))
+            nat.check(L.fvdbm_mp_spmm(P(g["At"][0]), P(g["At"][1]), P(g["At"][2]), n, P(g["dm"]), H, P(g["dh"]), 1, s))
+        nat.check(L.fvdbm_mp_relu_bwd(P(g["dh"]), P(g["z"][0]), P(g["dz"]), n * H, s))
+        nat.check(L.fvdbm_mp_dense_bwd_weight(P(g["dz"]), n, H, P(g["x"]), NFEAT, 0, 0, self._w(0, G), self._b(0, G),
+                                              ws, wsn, s))
+
+    def loss_and_grads(self, g):
+        """Forward, mean squared error against g['t'] and backward into self.G."""
+        import torch
+        L, s, n = nat.lib(), self._stream(), g["n"]
+        if g.get("dy") is None:
+            g["dy"] = torch.empty((n, NOUT), device=self._dev)
+            nb = L.fvdbm_mp_mse_scratch(n * NOUT)
+            g["mscr"] = torch.empty((nb + 7) // 8, dtype=torch.float64, device=self._dev)
+        self._forward(g)
+        nat.check(L.fvdbm_mp_mse(self._p(g["y"]), self._p(g["t"]), 0, n * NOUT, float(n * NOUT), self._p(g["dy"]),
+                                 self._p(g["mscr"]), g["mscr"].numel() * 8, s))
+        self._backward(g, g["dy"])
+        return g["mscr"][0]
+
+    # -- training and prediction ------------------------------------------
+    def fit(self, samples, epochs: int = 1500, lr: float = 2e-3, lr_final: float = 1e-4, log_every: int = 100,
+            b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8):
+        """Full-batch Adam over all samples (their graphs joined); the learning
+        rate decays geometrically from lr to lr_final.  Returns the loss
+        history [(epoch, loss)]."""
+        x = np.concatenate([s.x for s in samples])
+        t = np.concatenate([s.t for s in samples])
+        self.x_mu, self.x_sd = x.mean(0), np.maximum(x.std(0), 1e-12)
+        self.t_mu, self.t_sd = t.mean(0), np.maximum(t.std(0), 1e-12)
+        g = self._upload(samples, True)
+        L, s = nat.lib(), self._stream()
+        hist = []
+        for ep in range(epochs):
+            loss = self.loss_and_grads(g)
+            self.step_count += 1
+            rate = lr * (lr_final / lr) ** (ep / max(epochs - 1, 1))
+            nat.check(L.fvdbm_mp_adam(self._p(self.P), self._p(self.M), self._p(self.V), self._p(self.Pb),
+                                      self._p(self.G), self.size, rate, b1, b2, eps, self.step_count, s))
+            if ep % log_every == 0 or ep == epochs - 1:
+                hist.append((ep, float(loss.item())))
+        return hist
+
+    def evaluate(self, samples):
+        g = self._upload(samples, True)
+        return float(self.loss_and_grads(g).item())
+
+    def predict(self, sample: Sample) -> np.ndarray:
+        """Network output (in target units, not standardised) [N,3]."""
+        g = self._upload([sample], False)
+        self._forward(g)
+        y = g["y"].detach().cpu().numpy()
+        return y * self.t_sd + self.t_mu
+
+    def save(self, path):
+        np.savez(path, P=self.P.detach().cpu().numpy(), x_mu=self.x_mu, x_sd=self.x_sd, t_mu=self.t_mu,
+                 t_sd=self.t_sd, hidden=self.hidden, layers=self.layers)
+
+    @classmethod
+    def load(cls, path, device: int = 0):
+        import torch
+        z = np.load(path)
+        net = cls(int(z["hidden"]), int(z["layers"]), device=device)
+        net.P.copy_(torch.from_numpy(z["P"]))
+        net._sync_bf16()
+        for k in ("x_mu", "x_sd", "t_mu", "t_sd"):
+            setattr(net, k, z[k])
+        return net
+
+
+# ----------------------------------------------------------------------------
+# solver side
+def sample(case, rho_in: float, rho_out: float, rho=None, vel=None) -> Sample:
+    """Sample of a case (dynamics, cells, faces, nodes, mesher); with the
+    steady rho/vel it carries the training targets."""
+    dyn, c, f, n, m = case
+    x = features(m, c, f, n, rho_in, rho_out)
+    t = None if rho is None else targets(rho, vel, rho_in, rho_out)
+    return Sample(x, cell_graph(f, x.shape[0]), t)
+
+
+def macros(pdf):
+    """rho, u of cell pdfs [N,9] (src/dynamics.py:35-47), for targets and checks."""
+    from .dynamics import D2Q9
+    pdf = np.asarray(pdf, np.float64)
+    rho = pdf.sum(1)
+    return rho, (pdf @ D2Q9.KSI.astype(np.float64)) / rho[:, None]
+
+
+def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, stall_checks: int = 20,
+              stall_factor: float = 0.9):
+    """Steps a Batch to steady state with per-case retirement, like
+    ``Batch.run_to_steady``, and with the warm-start fallback: when ``init`` =
+    (rho [N], vel [N,2]) is given every case starts from feq(rho, u), and a
+    case whose residual after ``stall_checks`` checks is not below
+    ``stall_factor`` times its value ``stall_checks`` checks earlier restarts
+    from the uniform state feq(1, 0).  Returns per-case steps (including the
+    steps before a restart), status (1 converged, 0 cap, 2 non-finite) and the
+    restart flags."""
+    S = batch.n_cases
+    if init is not None:
+        batch.set_cells_eq(*init)
+    steps = np.zeros(S, np.int64)
+    status = np.zeros(S, np.int32)
+    restarted = np.zeros(S, bool)
+    active = np.ones(S, bool)
+    hist = [[] for _ in range(S)]
+    batch.set_active(active.astype(np.int32))
+    batch.residual()
+    while active.any():
+        n = int(min(check_every, np.min(cap - steps[active])))
+        batch.step(n)
+        steps[active] += n
+        r, _ = batch.residual()
+        restart = []
+        for s in np.flatnonzero(active):
+            hist[s].append(r[s])
+            if np.isnan(r[s]):
+                status[s], active[s] = 2, False
+            elif r[s] < threshold:
+                status[s], active[s] = 1, False
+            elif steps[s] >= cap:
+                active[s] = False
+            elif (init is not None and not restarted[s] and len(hist[s]) > stall_checks
+                  and r[s] > stall_factor * hist[s][-1 - stall_checks]):
+                restart.append(s)
+        for s in restart:
+            from .dynamics import D2Q9
+            nc = int(batch.cell_ptr[s + 1] - batch.cell_ptr[s])
+            batch.set_case_pdf(s, np.tile(D2Q9.W.astype(np.float32), (nc, 1)))
+            restarted[s] = True
+            hist[s] = []
+        batch.set_active(active.astype(np.int32))
+        if restart:
+            batch.residual()  # new snapshot after the restart
+    return steps, status, restarted

@@ -134,6 +134,11 @@ int fvdbm_create(const fvdbm_mesh_t *mesh, const fvdbm_params_t *params, void **
 int fvdbm_set_state(void *handle, const float *cell_pdf, const float *node_pdf,
                     const float *node_rho, const float *node_vel);
 
+/* Cell pdfs set to the equilibrium of given macros, f = feq(rho, u)
+ * (src/dynamics.py:70-74, the form Container.__init__ uses for its default
+ * state, src/containers.py:24-30): the warm start.  rho [N], vel [N][2]. */
+int fvdbm_set_cells_eq(void *handle, const float *rho, const float *vel);
+
 /* n_steps applications of Environment.step (src/environment.py:55-65). */
 int fvdbm_step(void *handle, int32_t n_steps);
 

@@ -1,0 +1,75 @@
+/*
+ * fvdbm_mpnn.h - kernels of the learned warm start (libfvdbm.so).
+ *
+ * No counterpart in the reference, which initialises every case uniformly
+ * (every pdf = feq(1, 0), src/containers.py:24-30).  A small message-passing
+ * network predicts the steady rho and u of a case from per-cell geometry; the
+ * solver then starts from f = feq(rho, u) (fvdbm_set_cells_eq) and still runs
+ * to its residual threshold.
+ *
+ * Conventions: all array pointers are DEVICE pointers; activations are
+ * row-major float32 [n][width]; weights are bfloat16 bit patterns (uint16_t)
+ * row-major [out][in]; `stream` is a cudaStream_t (NULL = default stream).
+ * Calls are asynchronous on that stream.  Return 0, -1 for an invalid
+ * argument, -2 for a CUDA error.  Every sum runs in a fixed order, so the
+ * results are bitwise reproducible.
+ */
+#ifndef FVDBM_MPNN_H
+#define FVDBM_MPNN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Dense layer, forward: z = [xa | xb] W^T + bias; y = relu(z) if relu else z,
+ * plus residual when given.  da + db <= 128, dout <= 128.  z (pre-activation)
+ * is stored when non-NULL; xb/bias/residual may be NULL (db = 0). */
+int fvdbm_mp_dense_fwd(const float *xa, int32_t da, const float *xb, int32_t db, int32_t n, const uint16_t *w,
+                       const float *bias, int32_t dout, int32_t relu, const float *residual, float *z, float *y,
+                       void *stream);
+
+/* Dense layer, backward to the inputs: [dxa | dxb] = dz W.  dxa is
+ * accumulated into when acc_a, else overwritten; dxb is overwritten. */
+int fvdbm_mp_dense_bwd_data(const float *dz, int32_t n, int32_t dout, const uint16_t *w, int32_t da, int32_t db,
+                            float *dxa, int32_t acc_a, float *dxb, void *stream);
+
+/* Dense layer, backward to the parameters: dw = dz^T [xa | xb] (float32
+ * [dout][da+db]) and dbias = column sums of dz (may be NULL).  scratch holds
+ * per-block partials: at least fvdbm_mp_wgrad_scratch(n, dout, da + db) bytes.
+ * dout * (da + db) + dout <= 8256. */
+size_t fvdbm_mp_wgrad_scratch(int32_t n, int32_t dout, int32_t din);
+int fvdbm_mp_dense_bwd_weight(const float *dz, int32_t n, int32_t dout, const float *xa, int32_t da,
+                              const float *xb, int32_t db, float *dw, float *dbias, float *scratch,
+                              size_t scratch_bytes, void *stream);
+
+/* dz = dy where z > 0, else 0 (count elements). */
+int fvdbm_mp_relu_bwd(const float *dy, const float *z, float *dz, size_t count, void *stream);
+
+/* Neighbour aggregation: out[i][:] (+)= sum_e wt[e] h[col[e]][:] over the CSR
+ * row i (row_ptr [n+1]), in entry order. */
+int fvdbm_mp_spmm(const int32_t *row_ptr, const int32_t *col, const float *wt, int32_t n, const float *h,
+                  int32_t d, float *out, int32_t accumulate, void *stream);
+
+/* Masked mean squared error: loss = sum mask (y - t)^2 / mask_total into
+ * scratch[0] (double, device); dy = 2 mask (y - t) / mask_total.  mask may be
+ * NULL (all ones).  scratch: at least fvdbm_mp_mse_scratch(count) bytes. */
+size_t fvdbm_mp_mse_scratch(size_t count);
+int fvdbm_mp_mse(const float *y, const float *t, const float *mask, size_t count, float mask_total, float *dy,
+                 double *scratch, size_t scratch_bytes, void *stream);
+
+/* Adam step `step` (1-based) on float32 master weights w with moments m, v;
+ * wb (may be NULL) receives w rounded to bfloat16 (nearest even). */
+int fvdbm_mp_adam(float *w, float *m, float *v, uint16_t *wb, const float *g, size_t count, float lr, float b1,
+                  float b2, float eps, int32_t step, void *stream);
+
+/* y = x rounded to bfloat16 (nearest even). */
+int fvdbm_mp_to_bf16(const float *x, uint16_t *y, size_t count, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FVDBM_MPNN_H */

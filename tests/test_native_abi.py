@@ -1,7 +1,8 @@
 """The C-ABI library builds for sm_103a, loads, exports every entry point
-that include/fvdbm.h declares, and rejects invalid containers in host-side
+that include/*.h declares, and rejects invalid containers in host-side
 validation (which runs before any CUDA call, so no GPU is needed)."""
 import ctypes as C
+import glob
 import os
 import re
 
@@ -10,17 +11,19 @@ import pytest
 
 from fvdbm_jax_gb300 import _native as nat
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "fvdbm.h")
+HEADERS = sorted(glob.glob(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                                        "*.h")))
 
 
 def declared():
-    src = open(HEADER).read()
+    src = "".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(fvdbm_\w+)\s*\(", src, re.M)))
 
 
 def test_header_declares_the_boundary():
     names = declared()
-    for n in ("fvdbm_create", "fvdbm_step", "fvdbm_set_state", "fvdbm_get_cells", "fvdbm_destroy"):
+    for n in ("fvdbm_create", "fvdbm_step", "fvdbm_set_state", "fvdbm_get_cells", "fvdbm_destroy",
+              "fvdbm_batch_create", "fvdbm_residual", "fvdbm_mp_dense_fwd", "fvdbm_mp_adam"):
         assert n in names
 
 
