@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="porous1m",
-                    choices=["porous1m", "porous2m", "porous4m", "cavity", "channel", "batch"])
+                    choices=["porous1m", "porous2m", "porous4m", "cavity", "channel", "batch", "warmstart"])
     ap.add_argument("--flux", default="upwind", choices=["upwind", "lax_wendroff"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--threshold", type=float, default=1e-6)
     ap.add_argument("--check-every", type=int, default=100)
     ap.add_argument("--step-cap", type=int, default=20000)
+    # --workload warmstart: learned warm start against the uniform start
+    ap.add_argument("--train-cases", type=int, default=256)
+    ap.add_argument("--eval-cases", type=int, default=64)
+    ap.add_argument("--epochs", type=int, default=1500)
     return ap.parse_args()
 
 
@@ -477,12 +481,117 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def _ws_case(spec):
+    from fvdbm_jax_gb300 import cases as CS
+    return CS.porous_square(spec["obstacles"], spec["n_target"], spec["tau"], rho_in=spec["rho_in"],
+                            rho_out=spec["rho_out"], porosity=spec["porosity"], delta_t=spec["dt"],
+                            seed=spec["seed"], mesher=True)
+
+
+def run_warmstart(args):
+    """Learned warm start: solver-generated steady states of seeded porous
+    squares train the network (on the GPU, by the library's kernels); on
+    held-out geometries the solver runs to the residual threshold from the
+    uniform start and from f = feq(predicted rho, u), with the stall fallback,
+    both as one Batch with the same loop.  Reports steps and seconds."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+
+    import numpy as np
+    import torch
+
+    from fvdbm_jax_gb300 import Batch
+    from fvdbm_jax_gb300 import warmstart as WS
+
+    rng = np.random.default_rng(2024)
+
+    def spec(i):
+        return {"obstacles": int(rng.integers(10, 41)), "n_target": int(rng.uniform(4000, 8000)), "tau": 0.65,
+                "rho_in": float(rng.uniform(1.01, 1.05)), "rho_out": float(rng.uniform(0.95, 0.99)),
+                "porosity": float(rng.uniform(0.75, 0.85)), "dt": 1.0, "seed": 50_000 + i}
+    specs = [spec(i) for i in range(args.train_cases + args.eval_cases)]
+    t0 = time.perf_counter()
+    with cf.ProcessPoolExecutor(min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        allc = list(ex.map(_ws_case, specs, chunksize=4))
+    setup_s = time.perf_counter() - t0
+    train, evalc = allc[:args.train_cases], allc[args.train_cases:]
+    tspec, espec = specs[:args.train_cases], specs[args.train_cases:]
+    thr, every, cap = args.threshold, args.check_every, args.step_cap
+
+    # training data: the solver's own steady states
+    t = time.perf_counter()
+    b = Batch([c[1:4] for c in train])
+    b.init()
+    steps_t, res_t, st_t = b.run_to_steady(thr, every, cap)
+    state = b.state()
+    data_s = time.perf_counter() - t
+    samples = []
+    for s, (case, sp) in enumerate(zip(train, tspec)):
+        if st_t[s] != 1:
+            continue
+        rho, vel = WS.macros(b.case_state(s, state)["pdf"])
+        samples.append(WS.sample(case, sp["rho_in"], sp["rho_out"], rho, vel))
+    b.close()
+    t = time.perf_counter()
+    net = WS.MPNN(seed=0)
+    hist = net.fit(samples, epochs=args.epochs, lr=3e-3, log_every=max(args.epochs // 10, 1))
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t
+
+    # held-out: uniform start against the predicted start
+    def timed(init):
+        bb = Batch([c[1:4] for c in evalc])
+        bb.init()
+        bb.sync()
+        t1 = time.perf_counter()
+        out = WS.run_cases(bb, thr, every, cap, init=init)
+        bb.sync()
+        el = time.perf_counter() - t1
+        fin = bb.state()
+        bb.close()
+        return out, el, fin
+    (sp_, stp, _), plain_s, fin_p = timed(None)
+    rho, vel = [], []
+    t = time.perf_counter()
+    for case, sp in zip(evalc, espec):
+        y = net.predict(WS.sample(case, sp["rho_in"], sp["rho_out"]))
+        r, v = WS.untarget(y, sp["rho_in"], sp["rho_out"])
+        rho.append(r)
+        vel.append(v)
+    infer_s = time.perf_counter() - t
+    (sw, stw, restarted), warm_s, fin_w = timed((np.concatenate(rho), np.concatenate(vel)))
+    # accuracy of the prediction against the plain run's steady state
+    rho_p, vel_p = WS.macros(fin_p["pdf"])
+    pr, pv = np.concatenate(rho), np.concatenate(vel)
+    drho = np.concatenate([np.full(c[1].pdf.shape[0], s["rho_in"] - s["rho_out"]) for c, s in zip(evalc, espec)])
+    line = {"metric": f"time-to-steady @{thr:g} resid, warm vs plain (held-out porous squares)",
+            "value": round(warm_s, 3), "unit": "s", "higher_is_better": False,
+            "plain_s": round(plain_s, 3), "speedup_time": round(plain_s / warm_s, 2),
+            "steps_plain": int(sp_.sum()), "steps_warm": int(sw.sum()),
+            "speedup_steps": round(float(sp_.sum()) / max(float(sw.sum()), 1.0), 2),
+            "converged_plain": int(np.sum(stp == 1)), "converged_warm": int(np.sum(stw == 1)),
+            "restarts": int(restarted.sum()), "inference_s": round(infer_s, 3),
+            "pred_rel_err_rho": round(float(np.sqrt(np.mean(((pr - rho_p) / drho) ** 2))), 4),
+            "pred_rel_err_u": round(float(np.linalg.norm(pv - vel_p) / np.linalg.norm(vel_p)), 4),
+            "train": {"cases": len(samples), "cells": int(sum(s.n for s in samples)), "epochs": args.epochs,
+                      "loss": hist, "train_s": round(train_s, 2), "data_s": round(data_s, 2),
+                      "data_steps_median": int(np.median(steps_t))},
+            "n_gpus": 1, "dtype": "f32 solver; bf16 weights / f32 accumulate network", "data": "synthetic",
+            "config": {"workload": f"porous squares, 10-40 obstacles, porosity 0.75-0.85, 4k-8k cells, "
+                                   f"rho_in 1.01-1.05 / rho_out 0.95-0.99, tau 0.65, dt 1.0, upwind; "
+                                   f"{args.train_cases} training + {args.eval_cases} held-out geometries",
+                       "check_every": every, "step_cap": cap, "setup_s": round(setup_s, 1)}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "warmstart":
+        run_warmstart(args)
     else:
         run_gb300(args)
 
