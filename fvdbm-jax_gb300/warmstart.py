@@ -13,9 +13,14 @@ device memory and the stream.
 
 Network (hidden 64, 4 message-passing layers):
     h0 = relu(x W0^T + b0)
-    m_l = A h_{l-1};  h_l = h_{l-1} + relu([h_{l-1} | m_l] W_l^T + b_l)
+    m_l = A_l h_{l-1};  h_l = h_{l-1} + relu([h_{l-1} | m_l] W_l^T + b_l)
     y = h_4 W_out^T + b_out
-with A the mean over a cell's neighbours through interior faces.  Per-cell
+Layer l's messages come from one of two kinds of neighbourhood (``SCALES``):
+"mesh", the mean over a cell's neighbours through interior faces, or a
+coarse grid of g x g bins over the case, where the message is the mean over
+the cell's bin (cell -> bin -> cell, two sparse stages).  The grid layers let
+four layers see the whole domain: the steady velocity in a pore depends on
+the flow paths through the whole sample, not only on the cells nearby.  Per-cell
 features x: centroid (2), distance to the nearest wall, area, inlet and
 outlet density; outputs: (rho - rho_out)/drho, u/drho (drho = rho_in - rho_out),
 each standardised over the training set.
@@ -27,13 +32,27 @@ import numpy as np
 from . import _native as nat
 
 HIDDEN, LAYERS, NFEAT, NOUT = 64, 4, 6, 3
+# neighbourhood of each message-passing layer: mesh neighbours, then count-aware
+# bins of 16 x 16, 4 x 4 and 1 x 1 (the whole sample)
+SCALES = ("mesh", "c16", "c4", "c1")
 
 
 # ----------------------------------------------------------------------------
 # graph and features
-def cell_graph(faces, n_cells: int):
-    """Row-normalised adjacency through interior faces: CSR (row_ptr, col, wt)
-    of A and of A^T, each row's entries in ascending column order."""
+def _stage(S):
+    """One sparse stage of a layer's aggregation: the CSR of S and of S^T
+    (row_ptr, col, wt), each row's entries in ascending column order."""
+    S = S.tocsr().astype(np.float32)
+    S.sort_indices()
+    St = S.T.tocsr()
+    St.sort_indices()
+    pack = lambda M: (M.indptr.astype(np.int32), M.indices.astype(np.int32), M.data.astype(np.float32))
+    return {"rows": S.shape[0], "cols": S.shape[1], "M": pack(S), "Mt": pack(St)}
+
+
+def mesh_mean(faces, n_cells: int):
+    """Row-normalised adjacency through interior faces (a cell without
+    neighbours gets a zero row)."""
     import scipy.sparse as sp
     fc = np.asarray(faces.stencil_cells_index, np.int64)
     inner = (fc[:, 0] >= 0) & (fc[:, 1] >= 0) & (fc[:, 0] != fc[:, 1])
@@ -44,13 +63,39 @@ def cell_graph(faces, n_cells: int):
     M.sum_duplicates()
     M.data[:] = 1.0
     deg = np.asarray(M.sum(1)).reshape(-1)
-    A = sp.diags(np.where(deg > 0, 1.0 / np.maximum(deg, 1), 0.0)) @ M
-    A = A.tocsr().astype(np.float32)
-    A.sort_indices()
-    At = A.T.tocsr()
-    At.sort_indices()
-    pack = lambda S: (S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.float32))
-    return pack(A), pack(At)
+    return (sp.diags(np.where(deg > 0, 1.0 / np.maximum(deg, 1), 0.0)) @ M).tocsr()
+
+
+def grid_mean(centers, g: int, counted: bool = False):
+    """The two stages of a bin mean on a g x g grid over the cells' bounding
+    box: P [bins, N] (mean of the bin's cells) and U [N, bins] (back to the
+    cells).  counted: P sums the bin's cells, divided by the mean bin
+    population, so that the message also says how full the bin is (the
+    solid fraction of that part of the sample)."""
+    import scipy.sparse as sp
+    c = np.asarray(centers, np.float64)
+    lo, hi = c.min(0), c.max(0)
+    ij = np.clip(((c - lo) / np.maximum(hi - lo, 1e-30) * g).astype(np.int64), 0, g - 1)
+    b = ij[:, 0] * g + ij[:, 1]
+    n = c.shape[0]
+    cnt = np.bincount(b, minlength=g * g).astype(np.float64)
+    w = np.full(n, g * g / n) if counted else 1.0 / cnt[b]
+    P = sp.csr_matrix((w, (b, np.arange(n))), shape=(g * g, n))
+    U = sp.csr_matrix((np.ones(n), (np.arange(n), b)), shape=(n, g * g))
+    return P, U
+
+
+def aggregations(faces, centers, n_cells: int, scales=SCALES):
+    """Per layer, the list of sparse stages whose product is A_l."""
+    out = []
+    for sc in scales:
+        if sc == "mesh":
+            out.append([_stage(mesh_mean(faces, n_cells))])
+        else:  # "c<g>": count-aware bins
+            counted = isinstance(sc, str) and sc.startswith("c")
+            P, U = grid_mean(centers, int(sc[1:]) if counted else int(sc), counted)
+            out.append([_stage(P), _stage(U)])
+    return out
 
 
 def wall_distance(mesher, faces, nodes):
@@ -92,30 +137,42 @@ def untarget(y, rho_in: float, rho_out: float):
 
 
 class Sample:
-    """One case for the network: features, adjacency and (for training) targets."""
+    """One case for the network: features, per-layer aggregation stages and
+    (for training) targets."""
 
-    def __init__(self, x, graph, t=None):
+    def __init__(self, x, aggs, t=None):
         self.x = np.asarray(x, np.float32)
-        self.A, self.At = graph
+        self.aggs = aggs
         self.t = None if t is None else np.asarray(t, np.float32)
         self.n = self.x.shape[0]
 
 
+def _cat_csr(mats, rows, cols):
+    """Block-diagonal union of CSR matrices (row/column sizes per block)."""
+    ptr, col, wt, off_e, off_c = [np.zeros(1, np.int32)], [], [], 0, 0
+    for (p, c, w), nc in zip(mats, cols):
+        ptr.append(p[1:] + off_e)
+        col.append(c + off_c)
+        wt.append(w)
+        off_e += int(p[-1])
+        off_c += nc
+    return np.concatenate(ptr).astype(np.int32), np.concatenate(col).astype(np.int32), np.concatenate(wt)
+
+
 def _concat(samples):
-    """Block-diagonal union of several samples' graphs."""
-    def cat(k):
-        ptr, col, wt, off_r, off_c = [np.zeros(1, np.int32)], [], [], 0, 0
-        for s in samples:
-            p, c, w = getattr(s, k)
-            ptr.append(p[1:] + off_r)
-            col.append(c + off_c)
-            wt.append(w)
-            off_r += int(p[-1])
-            off_c += s.n
-        return np.concatenate(ptr), np.concatenate(col), np.concatenate(wt)
+    """Block-diagonal union of several samples' aggregation stages."""
+    layers = []
+    for l in range(len(samples[0].aggs)):
+        stages = []
+        for k in range(len(samples[0].aggs[l])):
+            st = [s.aggs[l][k] for s in samples]
+            rows, cols = [x["rows"] for x in st], [x["cols"] for x in st]
+            stages.append({"rows": sum(rows), "cols": sum(cols), "M": _cat_csr([x["M"] for x in st], rows, cols),
+                           "Mt": _cat_csr([x["Mt"] for x in st], cols, rows)})
+        layers.append(stages)
     x = np.concatenate([s.x for s in samples])
     t = None if samples[0].t is None else np.concatenate([s.t for s in samples])
-    return x, cat("A"), cat("At"), t
+    return x, layers, t
 
 
 # ----------------------------------------------------------------------------
@@ -123,9 +180,12 @@ class MPNN:
     """The warm-start network; parameters live on the GPU (float32 master,
     bfloat16 copy used by the kernels)."""
 
-    def __init__(self, hidden: int = HIDDEN, layers: int = LAYERS, seed: int = 0, device: int = 0):
+    def __init__(self, hidden: int = HIDDEN, layers: int = LAYERS, seed: int = 0, device: int = 0,
+                 scales=SCALES):
         import torch
-        self.hidden, self.layers, self.device = hidden, layers, device
+        if len(scales) != layers:
+            raise ValueError("one neighbourhood scale per layer")
+        self.hidden, self.layers, self.device, self.scales = hidden, layers, device, tuple(scales)
         self.shapes = [((hidden, NFEAT), (hidden,))] + [((hidden, 2 * hidden), (hidden,))] * layers + \
                       [((NOUT, hidden), (NOUT,))]
         self.offs = []
@@ -202,12 +262,21 @@ class MPNN:
     # -- device batch ---------------------------------------------------------
     def _upload(self, samples, with_targets: bool):
         import torch
-        x, A, At, t = _concat(samples)
+        x, layers, t = _concat(samples)
         xn = (x - self.x_mu) / self.x_sd
         d = self._dev
-        g = {"n": x.shape[0], "x": torch.from_numpy(np.ascontiguousarray(xn, np.float32)).to(d),
-             "A": [torch.from_numpy(np.ascontiguousarray(a)).to(d) for a in A],
-             "At": [torch.from_numpy(np.ascontiguousarray(a)).to(d) for a in At]}
+        dev = lambda trip: [torch.from_numpy(np.ascontiguousarray(a)).to(d) for a in trip]
+        H = self.hidden
+        g = {"n": x.shape[0], "x": torch.from_numpy(np.ascontiguousarray(xn, np.float32)).to(d), "agg": []}
+        for stages in layers:
+            ag = []
+            for k, st in enumerate(stages):
+                last = k == len(stages) - 1
+                ag.append({"rows": st["rows"], "cols": st["cols"], "M": dev(st["M"]), "Mt": dev(st["Mt"]),
+                           # forward output of a stage before the last; its gradient
+                           "tmp": None if last else torch.empty((st["rows"], H), device=d),
+                           "gtmp": None if k == 0 else torch.empty((st["cols"], H), device=d)})
+            g["agg"].append(ag)
         if with_targets:
             tn = (t - self.t_mu) / self.t_sd
             g["t"] = torch.from_numpy(np.ascontiguousarray(tn, np.float32)).to(d)
@@ -225,7 +294,12 @@ class MPNN:
                                        P(g["z"][0]), P(g["h"][0]), s))
         for l in range(1, self.layers + 1):
             hp = g["h"][l - 1]
-            nat.check(L.fvdbm_mp_spmm(P(g["A"][0]), P(g["A"][1]), P(g["A"][2]), n, P(hp), H, P(g["m"][l - 1]), 0, s))
+            src = hp
+            for st in g["agg"][l - 1]:
+                dst = st["tmp"] if st["tmp"] is not None else g["m"][l - 1]
+                M = st["M"]
+                nat.check(L.fvdbm_mp_spmm(P(M[0]), P(M[1]), P(M[2]), st["rows"], P(src), H, P(dst), 0, s))
+                src = dst
             nat.check(L.fvdbm_mp_dense_fwd(P(hp), H, P(g["m"][l - 1]), H, n, self._w(l), self._b(l), H, 1, P(hp),
                                            P(g["z"][l]), P(g["h"][l]), s))
         lo = self.layers + 1
@@ -254,7 +328,16 @@ class MPNN:
             nat.check(L.fvdbm_mp_dense_bwd_weight(P(g["dz"]), n, H, P(g["h"][l - 1]), H, P(g["m"][l - 1]), H,
                                                   self._w(l, G), self._b(l, G), ws, wsn, s))
             nat.check(L.fvdbm_mp_dense_bwd_data(P(g["dz"]), n, H, self._w(l), H, H, P(g["dh"]), 1, P(g["dm"]), s))
-            nat.check(L.fvdbm_mp_spmm(P(g["At"][0]), P(g["At"][1]), P(g["At"][2]), n, P(g["dm"]), H, P(g["dh"]), 1, s))
+            grad = g["dm"]
+            for k in range(len(g["agg"][l - 1]) - 1, -1, -1):
+                st = g["agg"][l - 1][k]
+                Mt = st["Mt"]
+                if k == 0:  # back to the cells: accumulate into dh
+                    nat.check(L.fvdbm_mp_spmm(P(Mt[0]), P(Mt[1]), P(Mt[2]), st["cols"], P(grad), H, P(g["dh"]), 1, s))
+                else:
+                    nat.check(L.fvdbm_mp_spmm(P(Mt[0]), P(Mt[1]), P(Mt[2]), st["cols"], P(grad), H, P(st["gtmp"]),
+                                              0, s))
+                    grad = st["gtmp"]
         nat.check(L.fvdbm_mp_relu_bwd(P(g["dh"]), P(g["z"][0]), P(g["dz"]), n * H, s))
         nat.check(L.fvdbm_mp_dense_bwd_weight(P(g["dz"]), n, H, P(g["x"]), NFEAT, 0, 0, self._w(0, G), self._b(0, G),
                                               ws, wsn, s))
@@ -309,13 +392,14 @@ class MPNN:
 
     def save(self, path):
         np.savez(path, P=self.P.detach().cpu().numpy(), x_mu=self.x_mu, x_sd=self.x_sd, t_mu=self.t_mu,
-                 t_sd=self.t_sd, hidden=self.hidden, layers=self.layers)
+                 t_sd=self.t_sd, hidden=self.hidden, layers=self.layers, scales=np.array([str(s) for s in self.scales]))
 
     @classmethod
     def load(cls, path, device: int = 0):
         import torch
         z = np.load(path)
-        net = cls(int(z["hidden"]), int(z["layers"]), device=device)
+        scales = tuple(s if (s == "mesh" or s.startswith("c")) else int(s) for s in z["scales"])
+        net = cls(int(z["hidden"]), int(z["layers"]), device=device, scales=scales)
         net.P.copy_(torch.from_numpy(z["P"]))
         net._sync_bf16()
         for k in ("x_mu", "x_sd", "t_mu", "t_sd"):
@@ -325,13 +409,13 @@ class MPNN:
 
 # ----------------------------------------------------------------------------
 # solver side
-def sample(case, rho_in: float, rho_out: float, rho=None, vel=None) -> Sample:
+def sample(case, rho_in: float, rho_out: float, rho=None, vel=None, scales=SCALES) -> Sample:
     """Sample of a case (dynamics, cells, faces, nodes, mesher); with the
     steady rho/vel it carries the training targets."""
     dyn, c, f, n, m = case
     x = features(m, c, f, n, rho_in, rho_out)
     t = None if rho is None else targets(rho, vel, rho_in, rho_out)
-    return Sample(x, cell_graph(f, x.shape[0]), t)
+    return Sample(x, aggregations(f, m.cell_centers, x.shape[0], scales), t)
 
 
 def macros(pdf):
@@ -342,8 +426,8 @@ def macros(pdf):
     return rho, (pdf @ D2Q9.KSI.astype(np.float64)) / rho[:, None]
 
 
-def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, stall_checks: int = 20,
-              stall_factor: float = 0.9):
+def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, stall_checks: int = 100,
+              stall_factor: float = 0.95):
     """Steps a Batch to steady state with per-case retirement, like
     ``Batch.run_to_steady``, and with the warm-start fallback: when ``init`` =
     (rho [N], vel [N,2]) is given every case starts from feq(rho, u), and a

@@ -11,9 +11,10 @@ to y [N,3]:
     y  = h_L W_out^T + b_out
     loss = sum((y - t)^2) / (3 N)
 
-A is the row-normalised cell adjacency (mean over the neighbours through
-interior faces).  Weights are the bfloat16 values the kernels use; the
-arithmetic here is float64.
+A_l is layer l's aggregation matrix (the mean over the neighbours through
+interior faces, or a bin mean on a coarse grid); ``A`` may be one matrix for
+every layer or a list with one per layer.  Weights are the bfloat16 values
+the kernels use; the arithmetic here is float64.
 """
 from __future__ import annotations
 
@@ -44,8 +45,9 @@ def forward(params, x, A):
     h = np.maximum(z, 0.0)
     cache["z"].append(z)
     cache["h"].append(h)
-    for W, b in mid:
-        m = A @ h
+    As = A if isinstance(A, (list, tuple)) else [A] * len(mid)
+    for (W, b), Al in zip(mid, As):
+        m = Al @ h
         z = np.concatenate([h, m], 1) @ W.T + b
         h = h + np.maximum(z, 0.0)
         cache["m"].append(m)
@@ -67,6 +69,7 @@ def loss_and_grads(params, x, A, t):
     hL = cache["h"][-1]
     grads[-1] = (dy.T @ hL, dy.sum(0))
     dh = dy @ Wo
+    As = A if isinstance(A, (list, tuple)) else [A] * (len(P) - 2)
     for l in range(len(P) - 2, 0, -1):
         W, _ = P[l]
         z, hp, m = cache["z"][l], cache["h"][l - 1], cache["m"][l - 1]
@@ -74,7 +77,7 @@ def loss_and_grads(params, x, A, t):
         grads[l] = (dz.T @ np.concatenate([hp, m], 1), dz.sum(0))
         dx = dz @ W
         d = hp.shape[1]
-        dh = dh + dx[:, :d] + A.T @ dx[:, d:]
+        dh = dh + dx[:, :d] + As[l - 1].T @ dx[:, d:]
     dz = dh * (cache["z"][0] > 0)
     grads[0] = (dz.T @ cache["x"], dz.sum(0))
     return loss, y, grads

@@ -11,7 +11,10 @@ pytestmark = pytest.mark.gpu
 
 
 def _random_sample(n=300, seed=0):
-    from fvdbm_jax_gb300.warmstart import Sample
+    """A random graph with layers of both kinds: mesh-like neighbour means
+    (layers 1, 2), count-aware bins on a 5 x 5 grid (layer 3) and bin means
+    on a 2 x 2 grid (layer 4)."""
+    from fvdbm_jax_gb300.warmstart import Sample, _stage, grid_mean
     rng = np.random.default_rng(seed)
     # random planar-ish graph: ring plus random chords, symmetric, mean weights
     nbr = [set() for _ in range(n)]
@@ -26,19 +29,21 @@ def _random_sample(n=300, seed=0):
     M = sp.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(n, n))
     deg = np.asarray(M.sum(1)).reshape(-1)
     A = (sp.diags(1.0 / deg) @ M).tocsr().astype(np.float32)
-    A.sort_indices()
-    At = A.T.tocsr()
-    At.sort_indices()
-    pk = lambda S: (S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.float32))
+    xy = rng.uniform(0, 1, (n, 2))
+    P5, U5 = grid_mean(xy, 5, counted=True)
+    P2, U2 = grid_mean(xy, 2)
+    aggs = [[_stage(A)], [_stage(A)], [_stage(P5), _stage(U5)], [_stage(P2), _stage(U2)]]
+    dense = [A.toarray()] * 2 + [(U5.astype(np.float32) @ P5.astype(np.float32)).toarray(),
+                                 (U2.astype(np.float32) @ P2.astype(np.float32)).toarray()]
     x = rng.standard_normal((n, 6)).astype(np.float32)
     t = rng.standard_normal((n, 3)).astype(np.float32)
-    return Sample(x, (pk(A), pk(At)), t), A.toarray().astype(np.float64)
+    return Sample(x, aggs, t), [d.astype(np.float64) for d in dense]
 
 
 def test_forward_backward_match_oracle():
     from fvdbm_jax_gb300.warmstart import MPNN
     smp, A = _random_sample()
-    net = MPNN(seed=3)
+    net = MPNN(seed=3, scales=("mesh", "mesh", "c5", 2))
     g = net._upload([smp], True)  # identity feature/target scaling
     loss = float(net.loss_and_grads(g).item())
     y = g["y"].detach().cpu().numpy()
@@ -60,7 +65,7 @@ def test_training_is_reproducible_and_learns():
         np.float32)
     hists, params = [], []
     for _ in range(2):
-        net = MPNN(seed=11)
+        net = MPNN(seed=11, scales=("mesh", "mesh", "c5", 2))
         hists.append(net.fit([smp], epochs=300, lr=3e-3, log_every=50))
         params.append(net.get_params(rounded=False))
     assert hists[0] == hists[1]
