@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=100)
-    ap.add_argument("--kernel", default="auto", choices=["auto", "one", "fused", "staged", "tile", "tile_split"])
+    ap.add_argument("--kernel", default="auto",
+                    choices=["auto", "one", "fused", "fused_nodes", "staged", "tile", "tile_split"])
     # --workload batch: time-to-steady of many independent cases, batched vs one at a time
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--threshold", type=float, default=1e-6)
@@ -336,7 +337,7 @@ def run_gb300(args):
     # kernel does the whole step in one launch.
     F = info["n_faces"]
     K3 = int(np.asarray(c.face_indices).shape[1])
-    if info["kernel"] in (3, 5):
+    if info["kernel"] in (3, 5, 7):
         cell_bytes = info["bytes_per_step"]
     elif info["kernel"] == 4:
         cell_bytes = info["bytes_per_step"] - 36.0 * info["n_bc_nodes"]
@@ -389,7 +390,8 @@ def run_gb300(args):
     if rank == 0:
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                      "l2": "flushed between timed steps (2x L2 written, then read back, on the step's stream)",
-                     "kernel": {1: "staged", 2: "fused", 3: "tile", 4: "tile_split", 5: "one"}[info["kernel"]],
+                     "kernel": {1: "staged", 2: "fused", 3: "tile", 4: "tile_split", 5: "one",
+                                7: "fused_nodes"}[info["kernel"]],
                      "launches_per_step": info["launches_per_step"],
                      "ctas_per_sm": info["ctas_per_sm"]})
         line = {
@@ -399,7 +401,8 @@ def run_gb300(args):
             "config": desc,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": profiled_traffic("cell_kernel"),
-                         "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile", 4: "k_tile", 5: "k_step"}[info["kernel"]],
+                         "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile", 4: "k_tile", 5: "k_step",
+                                    7: "k_fused_nodes"}[info["kernel"]],
                          "bytes_per_launch": cell_bytes, "avg_launch_us": round(cell_avg_s * 1e6, 3),
                          "peak_kind": peak_kind,
                          "step_frac": round(step_achieved / peak, 4),

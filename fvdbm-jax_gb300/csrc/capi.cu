@@ -53,7 +53,14 @@ struct Handle {
   double* bred = nullptr;  // batch residual partials, then 4 totals per case
   int* status = nullptr;
   std::vector<float> node_pdf, node_rho, node_vel;  // reference-order host truth
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};  // [cur + 2 * node_cur]
+  // in-kernel node update (FVDBM_KERNEL_FUSED_NODES): two node buffers; the
+  // next step reads buffer node_cur and its kernel writes node_cur ^ 1;
+  // node_last holds the node state of the last step (or the upload)
+  bool fnodes = false;
+  float* nbuf[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  int node_cur = 0, node_last = 1;
+  bool nodes_ready = false;
   // convergence monitor (fvdbm_residual)
   float* usnap = nullptr;   // [2][Np] velocity at the previous residual call
   double* red = nullptr;    // chunk partials, then the 4 totals
@@ -168,6 +175,16 @@ int upload_nodes(Handle* h) {
   CK(cudaMemcpyAsync(h->dp.node_pdf, pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->dp.node_rho, rho.data(), rho.size() * 4, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->dp.node_vel, vel.data(), vel.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  if (h->fnodes) {
+    // both buffers hold the upload (and the set values of the computed nodes)
+    for (int b = 0; b < 2; ++b) {
+      CK(cudaMemcpyAsync(h->nbuf[b][0], pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      CK(cudaMemcpyAsync(h->nbuf[b][1], rho.data(), rho.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      CK(cudaMemcpyAsync(h->nbuf[b][2], vel.data(), vel.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+    h->nodes_ready = false;
+    h->node_last = h->node_cur ^ 1;
+  }
   // pageable sources: make sure the copies finished before the vectors die
   CK(cudaStreamSynchronize(h->stream));
   return FVDBM_OK;
@@ -176,11 +193,41 @@ int upload_nodes(Handle* h) {
 // Back-to-back steps use programmatic dependent launch between the node and
 // cell kernels (each waits for its predecessor before reading its output);
 // the first launch of a call follows whatever preceded it in the stream.
+// The plan with the node pointers of buffer a (read) and b (written).
+DevPlan with_nodes(const Handle* h, int a, int b) {
+  DevPlan q = h->dp;
+  q.node_pdf = h->nbuf[a][0];
+  q.node_rho = h->nbuf[a][1];
+  q.node_vel = h->nbuf[a][2];
+  q.node_pdf_nx = h->nbuf[b][0];
+  q.node_rho_nx = h->nbuf[b][1];
+  q.node_vel_nx = h->nbuf[b][2];
+  return q;
+}
+
+// In-kernel node update: the boundary nodes of the next step, computed once
+// from the recorded stencil macros after an upload (the step kernels then
+// keep them current).
+int ensure_nodes(Handle* h) {
+  if (!h->fnodes || h->nodes_ready) return FVDBM_OK;
+  CK(launch_nodes_cp(with_nodes(h, h->node_cur, h->node_cur), h->f[h->cur], h->stream, false));
+  h->nodes_ready = true;
+  return FVDBM_OK;
+}
+
 int enqueue_steps(Handle* h, int n) {
+  if (h->fnodes) {
+    int rc = ensure_nodes(h);
+    if (rc != FVDBM_OK) return rc;
+  }
   for (int s = 0; s < n; ++s) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
-    if (h->batch) {
+    if (h->fnodes) {
+      CK(launch_fused_nodes(with_nodes(h, h->node_cur, h->node_cur ^ 1), fin, fout, h->stream, /*pdl=*/true));
+      h->node_last = h->node_cur;
+      h->node_cur ^= 1;
+    } else if (h->batch) {
       CK(launch_nodes(h->dp, fin, h->stream, /*pdl=*/s > 0));
       CK(launch_fused_batch(h->dp, fin, fout, h->stream, /*pdl=*/h->dp.NB > 0 || s > 0, h->batch_block,
                             h->batch_waves));
@@ -216,17 +263,19 @@ int check_status(Handle* h) {
 }
 
 int get_graph(Handle* h, int parity, cudaGraphExec_t* out) {
+  parity += 2 * (h->fnodes ? h->node_cur : 0);
   if (h->graph[parity]) {
     *out = h->graph[parity];
     return FVDBM_OK;
   }
-  const int save = h->cur;
-  h->cur = parity;
+  const int save = h->cur, save_nc = h->node_cur, save_nl = h->node_last;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   int rc = enqueue_steps(h, kGraphSteps);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   h->cur = save;
+  h->node_cur = save_nc;
+  h->node_last = save_nl;
   if (rc != FVDBM_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -312,7 +361,12 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   Handle* h = new Handle();
   h->params = *params;
   h->device = params->device;
-  std::string why = build_plan(mesh, params, h->hp, segs);
+  // AUTO: the single-launch step (node update inside the fused cell kernel)
+  // when the mesh allows it, else the staged kernels
+  const bool auto_family = params->kernel == FVDBM_KERNEL_AUTO && !segs;
+  fvdbm_params_t pplan = *params;
+  if (auto_family) pplan.kernel = FVDBM_KERNEL_FUSED_NODES;
+  std::string why = build_plan(mesh, &pplan, h->hp, segs);
   if (!why.empty()) {
     h->err = why;
     return create_fail(h, FVDBM_EINVAL);
@@ -331,6 +385,13 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   const HostPlan& hp = h->hp;
   DevPlan& p = h->dp;
   h->fused = hp.fusable && params->kernel != FVDBM_KERNEL_STAGED;
+  if (params->kernel == FVDBM_KERNEL_FUSED_NODES && !(hp.fusable && hp.K == 3 && hp.stencil_first)) {
+    h->err = "the in-kernel node update needs triangles (3 face slots per cell), every cell face slot "
+             "naming a face of that cell, and no per-q flux scale";
+    return create_fail(h, FVDBM_EINVAL);
+  }
+  h->fnodes = params->kernel == FVDBM_KERNEL_FUSED_NODES ||
+              (auto_family && hp.fusable && hp.K == 3 && hp.stencil_first);
   const bool want_tile = params->kernel == FVDBM_KERNEL_TILE || params->kernel == FVDBM_KERNEL_TILE_SPLIT;
   if ((params->kernel == FVDBM_KERNEL_FUSED || want_tile) && !hp.fusable) {
     h->err = "the fused kernels need every cell face slot to name a face of that cell "
@@ -428,7 +489,10 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   UP(pn_meta, hp.pn_meta);
   UP(pn_sumw, hp.pn_sumw);
   p.stencil_start = hp.stencil_start;
-  p.Sp = std::max(32, (hp.N - hp.stencil_start + 31) / 32 * 32);
+  p.stencil_end = hp.stencil_end;
+  p.stencil_first = hp.stencil_first ? 1 : 0;
+  p.last_slot = hp.last_slot;
+  p.Sp = std::max(32, (hp.stencil_end - hp.stencil_start + 31) / 32 * 32);
   {
     float* d = nullptr;
     if ((rc = dalloc<float>(h, &d, size_t(12) * p.Sp)) != FVDBM_OK) return create_fail(h, rc);
@@ -469,6 +533,14 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     p.node_rho = d;
     if ((rc = dalloc<float>(h, &d, size_t(2) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
     p.node_vel = d;
+    h->nbuf[0][0] = p.node_pdf;
+    h->nbuf[0][1] = p.node_rho;
+    h->nbuf[0][2] = p.node_vel;
+    if (h->fnodes) {
+      const size_t sz[3] = {size_t(Q) * hp.Mp, size_t(hp.Mp), size_t(2) * hp.Mp};
+      for (int k = 0; k < 3; ++k)
+        if ((rc = dalloc<float>(h, &h->nbuf[1][k], sz[k])) != FVDBM_OK) return create_fail(h, rc);
+    }
   }
   for (int b = 0; b < 2; ++b) {
     if ((rc = dalloc<float>(h, &h->f[b], size_t(Q) * hp.Np)) != FVDBM_OK) return create_fail(h, rc);
@@ -704,6 +776,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
       if (!h->active[s])
         CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
     h->snap_step = -1;
+    h->nodes_ready = false;
   }
   if (node_pdf || node_rho || node_vel) {
     if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(Q) * hp.P * 4);
@@ -730,6 +803,7 @@ int fvdbm_set_cells_eq(void* handle, const float* rho, const float* vel) {
     if (!h->active[s])
       CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
   h->snap_step = -1;
+  h->nodes_ready = false;
   CK(cudaStreamSynchronize(h->stream));
   return FVDBM_OK;
 }
@@ -741,12 +815,15 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   CK(cudaSetDevice(h->device));
   int n = n_steps;
   if (n >= kGraphSteps && h->hp.N > 0) {
+    int rc = ensure_nodes(h);  // outside the capture
+    if (rc != FVDBM_OK) return rc;
     while (n >= kGraphSteps) {
       cudaGraphExec_t g;
-      int rc = get_graph(h, h->cur, &g);
+      rc = get_graph(h, h->cur, &g);
       if (rc != FVDBM_OK) return rc;
       CK(cudaGraphLaunch(g, h->stream));
-      n -= kGraphSteps;  // even: the current buffer is unchanged
+      n -= kGraphSteps;  // even: the current buffers are unchanged
+      if (h->fnodes) h->node_last = h->node_cur ^ 1;
     }
   }
   int rc = enqueue_steps(h, n);
@@ -783,6 +860,19 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   CK(cudaSetDevice(h->device));
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
+  if (h->fnodes) {
+    // one launch per step: phase 1 only brings the nodes up to date
+    if (phase == 1) return ensure_nodes(h);
+    if (phase != 2) return fail(h, FVDBM_EINVAL, "phase must be 1 or 2");
+    int rc = ensure_nodes(h);
+    if (rc != FVDBM_OK) return rc;
+    CK(launch_fused_nodes(with_nodes(h, h->node_cur, h->node_cur ^ 1), fin, fout, h->stream, false));
+    h->node_last = h->node_cur;
+    h->node_cur ^= 1;
+    h->cur ^= 1;
+    h->steps_done += 1;
+    return FVDBM_OK;
+  }
   if (phase == 1) {
     if (h->fused && !h->one && !h->tile)
       CK(launch_nodes_cp(h->dp, fin, h->stream, false));
@@ -870,9 +960,10 @@ int fvdbm_get_nodes(void* handle, float* pdf, float* rho, float* vel) {
   CK(cudaSetDevice(h->device));
   if (hp.M > 0) {
     std::vector<float> dp(size_t(Q) * hp.Mp), dr(hp.Mp), dv(size_t(2) * hp.Mp);
-    CK(cudaMemcpyAsync(dp.data(), h->dp.node_pdf, dp.size() * 4, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(dr.data(), h->dp.node_rho, dr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(dv.data(), h->dp.node_vel, dv.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    const DevPlan q = h->fnodes ? with_nodes(h, h->node_last, h->node_last) : h->dp;
+    CK(cudaMemcpyAsync(dp.data(), q.node_pdf, dp.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(dr.data(), q.node_rho, dr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(dv.data(), q.node_vel, dv.size() * 4, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (int d = 0; d < hp.M; ++d) {
       const int p = hp.node_orig[d];
@@ -898,7 +989,8 @@ int fvdbm_get_face_fluxes(void* handle, float* flux) {
     int rc = dalloc<float>(h, &h->flux, size_t(Q) * hp.Fp);
     if (rc != FVDBM_OK) return rc;
   }
-  CK(launch_face_flux(h->dp, h->f[h->cur ^ 1], h->flux, h->stream));
+  CK(launch_face_flux(h->fnodes ? with_nodes(h, h->node_last, h->node_last) : h->dp, h->f[h->cur ^ 1], h->flux,
+                      h->stream));
   std::vector<float> soa(size_t(Q) * hp.Fp);
   CK(cudaMemcpyAsync(soa.data(), h->flux, soa.size() * 4, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -974,10 +1066,10 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->batch ? FVDBM_KERNEL_BATCH : h->one ? FVDBM_KERNEL_ONE
+  info->kernel = h->fnodes ? FVDBM_KERNEL_FUSED_NODES : h->batch ? FVDBM_KERNEL_BATCH : h->one ? FVDBM_KERNEL_ONE
                          : h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
                                    : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
-  const int node_launch = (hp.Mc > 0 && !h->one && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
+  const int node_launch = (hp.Mc > 0 && !h->one && !h->fnodes && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
   info->launches_per_step = node_launch + (h->one || h->tile || h->batch ? 1 : (h->fused ? 1 : 2));
   info->padded_cells = hp.Np;
   info->ctas_per_sm = h->tile ? tile_ctas_per_sm(h->dp) : 0;

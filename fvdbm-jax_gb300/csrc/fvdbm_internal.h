@@ -92,7 +92,10 @@ struct HostPlan {
   std::vector<uint32_t> pe_slot;  // padded node-block tables (see plan.cpp)
   std::vector<float> pe_w, pn_sumw;
   std::vector<int32_t> pn_meta;
-  int stencil_start = 0;  // device cells [stencil_start, N) are node-stencil cells
+  int stencil_start = 0;  // device cells [stencil_start, stencil_end) are node-stencil cells
+  int stencil_end = 0;    // (last: [., N); first, for the in-kernel node update: [0, .))
+  bool stencil_first = false;
+  int last_slot = -1;     // cprod slot of the reference's last cell (stencil_first, padded nodes)
   std::vector<uint8_t> cblk_ghost;  // per 256-cell block: any ghost face
   std::vector<int32_t> sched;       // single-launch tickets: cell block >= 0, node block -(b+1)
 
@@ -200,7 +203,13 @@ struct DevPlan {
   int NB;
   // macros of the node-stencil cells [stencil_start, N): cprod[r][Sp] with
   // r = rho, ux, uy, f_q - feq_q; written by the fused kernel for the next step
-  int stencil_start, Sp;
+  int stencil_start, stencil_end, Sp;
+  int last_slot;
+  int stencil_first;
+  // in-kernel node update (k_fused_nodes): the next step's node buffers
+  float* node_pdf_nx;
+  float* node_rho_nx;
+  float* node_vel_nx;
   float* cprod;
   const unsigned* pe_slot;
   const float* pe_w;
@@ -249,6 +258,9 @@ cudaError_t launch_fused(const DevPlan& p, const float* fin, float* fout, cudaSt
                          bool pdl = false);
 // node kernel fed by the stencil macros the previous fused kernel recorded
 cudaError_t launch_nodes_cp(const DevPlan& p, const float* f, cudaStream_t s, bool pdl);
+// fused cell kernel that also computes the next step's boundary nodes (node
+// blocks in the grid wait, bounded, for the stencil cells' blocks)
+cudaError_t launch_fused_nodes(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl);
 // record the stencil macros of f (after an upload of the cell pdfs)
 cudaError_t launch_stencil_macros(const DevPlan& p, const float* f, cudaStream_t s);
 // the whole step in one launch (node blocks then cell blocks, see kernels.cu)

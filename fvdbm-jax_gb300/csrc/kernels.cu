@@ -135,13 +135,18 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
 // The same node evaluation, fed by the stencil macros that the previous
 // fused kernel recorded (cprod) instead of re-reading the stencil pdfs.  The
 // padded tables put a thread's entry and node record at blk*256 + tid, so the
-// first loads do not depend on one another.
-__global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes_cp(DevPlan p, const float* __restrict__ f) {
-  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
-  __shared__ float lastm[3];
-  grid_dep_launch();
+// first loads do not depend on one another.  Results go to npdf/nrho/nvel,
+// which also hold the set values (velocity of type-1, density of type-2
+// nodes).  Padded entries read the last cell's macros from f, or from cprod
+// when LAST_CPROD (the last cell is then a stencil cell).  WAIT: wait for the
+// previous kernel before reading cprod.
+template <bool WAIT, bool LAST_CPROD>
+__device__ __forceinline__ void node_block_cp(const DevPlan& p, int blk, const float* __restrict__ f,
+                                              float* __restrict__ npdf, float* __restrict__ nrho,
+                                              float* __restrict__ nvel, float (*prod)[NODE_BLOCK_ENTRIES],
+                                              float* lastm) {
   const int tid = threadIdx.x;
-  const size_t s = size_t(blockIdx.x) * NODE_BLOCK_ENTRIES + tid;
+  const size_t s = size_t(blk) * NODE_BLOCK_ENTRIES + tid;
   const unsigned slot = __ldg(p.pe_slot + s);
   const float w = __ldg(p.pe_w + s);
   const int4 nm = __ldg(reinterpret_cast<const int4*>(p.pn_meta) + s);  // node, first, count, type|npad
@@ -149,70 +154,87 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes_cp(DevPlan p, cons
   const int type = nm.w & 3;
   float set0 = 0.0f, set1 = 0.0f;
   if (type == 1) {
-    set0 = p.node_vel[nm.x];
-    set1 = p.node_vel[p.Mp + nm.x];
+    set0 = nvel[nm.x];
+    set1 = nvel[p.Mp + nm.x];
   } else if (type == 2) {
-    set0 = p.node_rho[nm.x];
+    set0 = nrho[nm.x];
   }
-  grid_dep_wait();  // cprod comes from the previous fused kernel
+  if (WAIT) grid_dep_wait();  // cprod comes from the previous fused kernel
   if (slot != ~0u) {
     const float* c = p.cprod + (slot & ~ND_NEQ_ZERO);
     const bool zero = (slot & ND_NEQ_ZERO) != 0;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) prod[r][tid] = __ldg(c + r * size_t(p.Sp)) * w;
+    for (int r = 0; r < 3; ++r) prod[r][tid] = __ldcg(c + r * size_t(p.Sp)) * w;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) prod[3 + q][tid] = (zero ? 0.0f : __ldg(c + (3 + q) * size_t(p.Sp))) * w;
+    for (int q = 0; q < Q; ++q) prod[3 + q][tid] = (zero ? 0.0f : __ldcg(c + (3 + q) * size_t(p.Sp))) * w;
   }
   if (tid == NODE_BLOCK_ENTRIES - 1) {
     // padded (-1, weight 0) entries gather the last cell
-    float fc[Q];
-    load_cell(f, p.last_cell, fc);
-    float rho, ux, uy;
-    macros(fc, rho, ux, uy);
-    lastm[0] = rho;
-    lastm[1] = ux;
-    lastm[2] = uy;
-  }
-  __syncthreads();
-  if (type == 0) return;
-  const int b = nm.y, cnt = nm.z;
-  float acc[12];
+    if (LAST_CPROD) {
+      if (p.last_slot >= 0)
 #pragma unroll
-  for (int r = 0; r < 12; ++r) acc[r] = 0.0f;
-  for (int k = 0; k < cnt; ++k) {
-#pragma unroll
-    for (int r = 0; r < 12; ++r) acc[r] = k ? acc[r] + prod[r][b + k] : prod[r][b + k];
-  }
-  if (nm.w & 4) {
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const float z = lastm[r] * 0.0f;
-      acc[r] = cnt ? acc[r] + z : z;
+        for (int r = 0; r < 3; ++r) lastm[r] = __ldcg(p.cprod + p.last_slot + r * size_t(p.Sp));
+    } else {
+      float fc[Q];
+      load_cell(f, p.last_cell, fc);
+      float rho, ux, uy;
+      macros(fc, rho, ux, uy);
+      lastm[0] = rho;
+      lastm[1] = ux;
+      lastm[2] = uy;
     }
   }
-  const int m = nm.x;
-  float rho_p, ux_p, uy_p;
-  if (type == 1) {
-    rho_p = acc[0] / sw;
-    ux_p = set0;
-    uy_p = set1;
-    p.node_rho[m] = rho_p;
-  } else {
-    rho_p = set0;
-    ux_p = acc[1] / sw;
-    uy_p = acc[2] / sw;
-    p.node_vel[m] = ux_p;
-    p.node_vel[p.Mp + m] = uy_p;
-  }
-  float eqn[Q];
-  feq9(rho_p, ux_p, uy_p, p, eqn);
+  __syncthreads();
+  if (type != 0) {  // (no early return: callers may synchronise after this)
+    const int b = nm.y, cnt = nm.z;
+    float acc[12];
 #pragma unroll
-  for (int q = 0; q < Q; ++q) p.node_pdf[size_t(q) * p.Mp + m] = eqn[q] + acc[3 + q] / sw;
+    for (int r = 0; r < 12; ++r) acc[r] = 0.0f;
+    for (int k = 0; k < cnt; ++k) {
+#pragma unroll
+      for (int r = 0; r < 12; ++r) acc[r] = k ? acc[r] + prod[r][b + k] : prod[r][b + k];
+    }
+    if (nm.w & 4) {
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const float z = lastm[r] * 0.0f;
+        acc[r] = cnt ? acc[r] + z : z;
+      }
+    }
+    const int m = nm.x;
+    float rho_p, ux_p, uy_p;
+    if (type == 1) {
+      rho_p = acc[0] / sw;
+      ux_p = set0;
+      uy_p = set1;
+      nrho[m] = rho_p;
+    } else {
+      rho_p = set0;
+      ux_p = acc[1] / sw;
+      uy_p = acc[2] / sw;
+      nvel[m] = ux_p;
+      nvel[p.Mp + m] = uy_p;
+    }
+    float eqn[Q];
+    feq9(rho_p, ux_p, uy_p, p, eqn);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) npdf[size_t(q) * p.Mp + m] = eqn[q] + acc[3 + q] / sw;
+  }
+}
+
+__global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes_cp(DevPlan p, const float* __restrict__ f) {
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  grid_dep_launch();
+  if (p.stencil_first)
+    node_block_cp<true, true>(p, blockIdx.x, f, p.node_pdf, p.node_rho, p.node_vel, prod, lastm);
+  else
+    node_block_cp<true, false>(p, blockIdx.x, f, p.node_pdf, p.node_rho, p.node_vel, prod, lastm);
 }
 
 __global__ void __launch_bounds__(256) k_stencil_macros(DevPlan p, const float* __restrict__ f) {
   const int i = p.stencil_start + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.N) return;
+  if (i >= p.stencil_end) return;
   float fc[Q];
   load_cell(f, i, fc);
   record_stencil(p, i, fc);
@@ -301,7 +323,7 @@ __device__ __forceinline__ void fused_cell_f(const DevPlan& p, const float* __re
     fn[q] = f[q] + dt * (inv_tau * (eq[q] - f[q]) - acc[q]);
     o[q * 32] = fn[q];
   }
-  if (RECORD && i >= p.stencil_start) record_stencil(p, i, fn);
+  if (RECORD && i >= p.stencil_start && i < p.stencil_end) record_stencil(p, i, fn);
 }
 
 template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG, bool RECORD = false>
@@ -351,6 +373,85 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
   fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
 }
 
+// Acquire load of a flag written by other blocks of the same launch.
+__device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+  return v;
+}
+
+// The fused cell kernel with the next step's boundary-node update in the same
+// launch.  The node-stencil cells come first (cell blocks [0, R) record their
+// new macros); the NB node blocks sit at grid position node_at.  A node block
+// waits (bounded; on timeout it sets the status word and skips its nodes)
+// until the R recording blocks have published, then evaluates its nodes from
+// the recorded macros into the next step's node buffers, while the remaining
+// cell blocks still run.  This step's ghost faces read the current node
+// buffers, written by the previous launch.  The last node block to finish
+// resets the two counters for the next launch.  At most NB blocks wait, far
+// fewer than the resident blocks, so the recording blocks always get an SM.
+template <int SCHEME, int VARIANT, bool FV>
+__global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __restrict__ fin,
+                                                     float* __restrict__ fout, int R, int node_at,
+                                                     int prefetch_blocks) {
+  constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+  static_assert(NODE_BLOCK_ENTRIES == 256, "node blocks use the whole CTA");
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  __shared__ int s_ok;
+  grid_dep_launch();
+  const int b = blockIdx.x;
+  int* ctr = p.step_ctr;  // [0] recording blocks published, [1] node blocks finished
+  if (b >= node_at && b < node_at + p.NB) {
+    grid_dep_wait();  // counters and set values of the previous launch
+    if (threadIdx.x == 0) {
+      int ok = 0;
+      for (int it = 0; it < (1 << 22); ++it) {
+        if (ld_acquire_gpu(&ctr[0]) >= R) {
+          ok = 1;
+          break;
+        }
+        __nanosleep(128);
+      }
+      if (!ok) atomicExch(p.status, STATUS_WAIT_TIMEOUT);
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (s_ok) node_block_cp<false, true>(p, b - node_at, fin, p.node_pdf_nx, p.node_rho_nx, p.node_vel_nx, prod, lastm);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (atomicAdd(&ctr[1], 1) == p.NB - 1) {
+        ctr[0] = 0;
+        ctr[1] = 0;
+        __threadfence();
+      }
+    }
+    return;
+  }
+  const int cb = b < node_at ? b : b - p.NB;
+  const int ncb = int(gridDim.x) - p.NB;
+  const int ahead = cb + prefetch_blocks;
+  const bool do_prefetch = threadIdx.x == 0 && prefetch_blocks > 0 && ahead < ncb;
+  const int pf_cells = do_prefetch ? min(256, p.Np - ahead * 256) : 0;
+  if (pf_cells > 0) prefetch_l2(p.hf + size_t(ahead) * 256 * HROWS, pf_cells * HROWS * sizeof(unsigned));
+  const int i = cb * 256 + threadIdx.x;
+  const unsigned* hb;
+  int code[3];
+  float nx[3], ny[3], Ls[3];
+  load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
+  grid_dep_wait();  // fin and the node pdfs come from the previous launch
+  if (pf_cells > 0) prefetch_l2(fin + size_t(ahead) * 256 * Q, pf_cells * Q * sizeof(float));
+  if (i < p.N) fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
+  if (cb < R) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(&ctr[0], 1);
+    }
+  }
+}
+
 // Packed batch of independent cases: the same cell update with the cell's
 // case's 1/tau and dt; cells of retired cases are neither read nor written
 // (both pdf buffers hold their final state).  Block size 128 or 256; the
@@ -392,11 +493,6 @@ __global__ void __launch_bounds__(256) k_fused_batch(DevPlan p, const float* __r
 // order, so every node ticket before a waiting block belongs to a block that
 // is already running: the wait cannot starve.  The last block to finish
 // resets the counters for the next launch.
-__device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
-  return v;
-}
 
 template <int SCHEME, int VARIANT, bool FV>
 __global__ void __launch_bounds__(256) k_step(DevPlan p, const float* __restrict__ fin,
@@ -667,7 +763,7 @@ cudaError_t launch_nodes_cp(const DevPlan& p, const float* f, cudaStream_t s, bo
 }
 
 cudaError_t launch_stencil_macros(const DevPlan& p, const float* f, cudaStream_t s) {
-  const int S = p.N - p.stencil_start;
+  const int S = p.stencil_end - p.stencil_start;
   if (S <= 0) return cudaSuccess;
   k_stencil_macros<<<blocks(S, 256), 256, 0, s>>>(p, f);
   return cudaGetLastError();
@@ -691,6 +787,32 @@ static cudaError_t fused_dispatch(const DevPlan& p, const float* fin, float* fou
   const int pf = fused_prefetch_blocks();
   if (p.fv) return launch_ex(k_fused<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, pf);
   return launch_ex(k_fused<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, pf);
+}
+
+template <int S, int V>
+static cudaError_t fused_nodes_dispatch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s,
+                                        bool pdl) {
+  const int ncb = blocks(p.N, 256);
+  const int R = p.NB > 0 ? blocks(p.stencil_end, 256) : 0;  // no node blocks: nothing to publish
+  // node blocks three quarters into the grid: the recording blocks are long
+  // done, and the node work overlaps the remaining cell blocks (measured on
+  // the 1M porous step: 35.3 us at 3/4 against 37.5 us one wave after the
+  // recording blocks and 37.4 us at the end)
+  const int node_at = std::min(ncb, std::max(R, ncb * 3 / 4));
+  const int pf = fused_prefetch_blocks();
+  if (p.fv)
+    return launch_ex(k_fused_nodes<S, V, true>, ncb + p.NB, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
+  return launch_ex(k_fused_nodes<S, V, false>, ncb + p.NB, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
+}
+
+cudaError_t launch_fused_nodes(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl) {
+  if (p.N == 0) return cudaSuccess;
+  if (p.K != 3 || !p.stencil_first) return cudaErrorInvalidValue;
+  if (p.scheme == 0 && p.variant == 0) return fused_nodes_dispatch<0, 0>(p, fin, fout, s, pdl);
+  if (p.scheme == 1 && p.variant == 0) return fused_nodes_dispatch<1, 0>(p, fin, fout, s, pdl);
+  if (p.scheme == 0 && p.variant == 1) return fused_nodes_dispatch<0, 1>(p, fin, fout, s, pdl);
+  if (p.scheme == 1 && p.variant == 1) return fused_nodes_dispatch<1, 1>(p, fin, fout, s, pdl);
+  return cudaErrorInvalidValue;
 }
 
 template <int S, int V>

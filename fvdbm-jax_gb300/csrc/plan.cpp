@@ -277,26 +277,46 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
   // step's node kernel, and the blocks that need boundary nodes in the
   // single-launch step form the tail of its grid.  (Not for the in-tile node
   // kernel, whose tiles must stay compact.)
+  // With the node update inside the fused kernel (KERNEL_FUSED_NODES) the
+  // stencil cells go first instead: their blocks finish early and the node
+  // blocks can run while the other cell blocks still compute.  The last
+  // reference cell then joins them when a node has padded entries (those
+  // read its macros).
   hp.stencil_start = N;
+  hp.stencil_end = N;
+  hp.stencil_first = pr.kernel == FVDBM_KERNEL_FUSED_NODES && !segs;
   if (N > 0 && Kn > 0 && pr.kernel != FVDBM_KERNEL_TILE && !segs) {
     std::vector<char> member(N, 0);
+    bool padded = false;
     for (int p_ = 0; p_ < P; ++p_) {
       if (m.node_type[p_] == 0) continue;
       for (int k = 0; k < Kn; ++k) {
         const int32_t c = m.node_cells[int64_t(p_) * Kn + k];
         float w = 1.0f / m.node_dists[int64_t(p_) * Kn + k];
         if (w < 0.0f) w = 0.0f;
-        if (c == -1 && w == 0.0f) continue;  // padding: evaluated from the last cell directly
+        if (c == -1 && w == 0.0f) {  // padding: evaluated from the last cell directly
+          padded = true;
+          continue;
+        }
         member[wrap(c, N)] = 1;
       }
     }
-    auto it = std::stable_partition(hp.cell_old.begin(), hp.cell_old.end(),
-                                    [&](int32_t c) { return !member[c]; });
-    hp.stencil_start = int(it - hp.cell_old.begin());
+    if (hp.stencil_first) {
+      if (padded) member[N - 1] = 1;
+      auto it = std::stable_partition(hp.cell_old.begin(), hp.cell_old.end(),
+                                      [&](int32_t c) { return member[c] != 0; });
+      hp.stencil_start = 0;
+      hp.stencil_end = int(it - hp.cell_old.begin());
+    } else {
+      auto it = std::stable_partition(hp.cell_old.begin(), hp.cell_old.end(),
+                                      [&](int32_t c) { return !member[c]; });
+      hp.stencil_start = int(it - hp.cell_old.begin());
+    }
   }
   hp.cell_new.assign(N, -1);
   for (int i = 0; i < N; ++i) hp.cell_new[hp.cell_old[i]] = i;
   hp.last_cell_new = N > 0 ? hp.cell_new[N - 1] : 0;
+  if (hp.stencil_first && hp.last_cell_new < hp.stencil_end) hp.last_slot = hp.last_cell_new - hp.stencil_start;
   auto cnew = [&](int32_t c) { return c < 0 ? -1 : hp.cell_new[c]; };
   auto cnew_wrap = [&](int32_t c) { return N > 0 ? hp.cell_new[wrap(c, N)] : 0; };
 

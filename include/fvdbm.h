@@ -65,6 +65,8 @@ extern "C" {
 #define FVDBM_KERNEL_TILE_SPLIT 4 /* node BC kernel + persistent tile kernel (2 kernels) */
 #define FVDBM_KERNEL_ONE 5        /* node and cell blocks in one launch (1 kernel) */
 #define FVDBM_KERNEL_BATCH 6      /* (reported by fvdbm_get_info) packed batch: node BC + fused cell kernel */
+#define FVDBM_KERNEL_FUSED_NODES 7 /* fused cell kernel that also updates the boundary nodes of the
+                                      next step (1 kernel) */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {

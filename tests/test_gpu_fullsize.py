@@ -68,7 +68,7 @@ def test_channel_config_bitwise(flux):
     from fvdbm_jax_gb300 import Environment, meshgen
     m, dyn, c, f, n = _case(meshgen.channel_cylinder(), flux, tau=0.55, bc="channel")
     ref = _oracle(c, f, n, dyn, 100)
-    for kernel in ("one", "tile", "tile_split", "fused", "staged"):
+    for kernel in ("one", "tile", "tile_split", "fused", "fused_nodes", "staged"):
         env = Environment(c, f, n, kernel=kernel)
         env.init()
         env.step(100)
@@ -91,20 +91,21 @@ def test_porous_1m_bitwise_and_deterministic():
     env2.init()
     env2.step(4)
     assert np.array_equal(np.array(env2.cells.pdf), a)
-    for kernel in ("one", "fused", "tile_split"):
+    for kernel in ("one", "fused", "fused_nodes", "tile_split"):
         env3 = Environment(c, f, n, kernel=kernel)
         env3.init()
         env3.step(4)
         assert np.array_equal(np.array(env3.cells.pdf), a), kernel
 
 
-def test_graph_and_eager_steps_agree():
+@pytest.mark.parametrize("kernel", ["auto", "fused_nodes"])
+def test_graph_and_eager_steps_agree(kernel):
     from fvdbm_jax_gb300 import Environment, meshgen
     m, dyn, c, f, n = _case(meshgen.cavity(n=21))
-    e1 = Environment(c, f, n)
+    e1 = Environment(c, f, n, kernel=kernel)
     e1.init()
     e1.step(70)            # 2 graph replays of 32 + 6 eager steps
-    e2 = Environment(c, f, n)
+    e2 = Environment(c, f, n, kernel=kernel)
     e2.init()
     for _ in range(70):
         e2.step()
@@ -112,10 +113,11 @@ def test_graph_and_eager_steps_agree():
     assert np.array_equal(np.array(e1.nodes.pdf), np.array(e2.nodes.pdf))
 
 
-def test_state_round_trip_and_midrun_write():
+@pytest.mark.parametrize("kernel", ["auto", "fused_nodes"])
+def test_state_round_trip_and_midrun_write(kernel):
     from fvdbm_jax_gb300 import Environment, meshgen
     m, dyn, c, f, n = _case(meshgen.cavity(n=15))
-    env = Environment(c, f, n)
+    env = Environment(c, f, n, kernel=kernel)
     env.init()
     rng = np.random.default_rng(0)
     pdf = (np.array(c.pdf) * (1 + 0.01 * rng.uniform(-1, 1, c.pdf.shape))).astype(np.float32)

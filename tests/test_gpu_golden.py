@@ -14,7 +14,8 @@ NOT_FUSABLE = {"mixed_quadtri_upwind", "cavity7_cc_alt_upwind"}
 def _cases():
     out = []
     for name in G.names():
-        kernels = ["staged", "auto"] if name in NOT_FUSABLE else ["one", "tile", "tile_split", "fused", "staged"]
+        kernels = ["staged", "auto"] if name in NOT_FUSABLE else ["one", "tile", "tile_split", "fused", "fused_nodes",
+                                                                  "staged"]
         for k in kernels:
             for order in ("none", "rcm", "morton"):
                 out.append((name, k, order))
