@@ -775,7 +775,7 @@ static int fused_prefetch_blocks() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cached = sms * 4;  // about one wave of 256-thread blocks
+    cached = sms * 2;  // half a wave of 256-thread blocks (measured best on the 1M step)
   }
   return cached;
 }
