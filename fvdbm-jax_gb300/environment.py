@@ -239,6 +239,29 @@ class Environment:
             pass
 
     # ------------------------------------------------------------------
+    # checkpoints: pickling keeps the containers with the current state (as
+    # the reference pickles its pytree, src/mesher.py:600-608); the device
+    # handle is not kept, and the next step re-initialises from that state,
+    # continuing the run exactly
+    def __getstate__(self):
+        import copy
+        if self._h is not None:
+            for cont, names in ((self.cells, ("pdf", "rho", "vel", "pdf_eq")), (self.faces, ("pdf",)),
+                                (self.nodes, ("pdf",))):
+                for nm in names:
+                    getattr(cont, nm)  # read the leaves back from the device
+        st = {k: v for k, v in self.__dict__.items() if k not in ("_h", "_fresh")}
+        for k in ("cells", "faces", "nodes"):
+            c = copy.copy(self.__dict__[k])
+            object.__setattr__(c, "_owner", None)
+            st[k] = c
+        st["_h"], st["_fresh"] = None, {}
+        return st
+
+    def __setstate__(self, st):
+        self.__dict__.update(st)
+
+    # ------------------------------------------------------------------
     # read-through of the dynamic leaves
     def _pull(self, cont: _Container, name: str):
         key = (id(cont), name)

@@ -299,6 +299,21 @@ class Mesher:
         return nodes
 
     # --- output -----------------------------------------------------------
+    def to_pickle(self, env, filename: str):
+        """Checkpoint (src/mesher.py:600-603): ``filename.pkl`` holds the
+        environment, with its current state, and this mesher."""
+        import pickle
+        with open(f"{filename}.pkl", "wb") as fh:
+            pickle.dump((env, self), fh)
+
+    @classmethod
+    def from_pickle(cls, filename: str):
+        """(env, mesher) from ``to_pickle`` (src/mesher.py:605-608); the
+        environment continues from the saved state at its next step."""
+        import pickle
+        with open(f"{filename}.pkl", "rb") as fh:
+            return pickle.load(fh)
+
     def to_vtk(self, env, filename: str, save_f: bool = False, save_feq: bool = False) -> str:
         """Legacy-ASCII VTK unstructured grid with cell ``Velocity`` (3-vector,
         z=0) and ``Density``, optionally ``pdf`` and ``feq`` (the fields the

@@ -160,3 +160,23 @@ def test_known_divisor_division_verified_and_used():
     env = Environment(c, f, n)
     env.init()
     assert env.info()["const_division"] == 1
+
+
+@pytest.mark.parametrize("kernel", ["auto", "fused"])
+def test_checkpoint_resume_is_exact(kernel, tmp_path):
+    from fvdbm_jax_gb300 import Environment, Mesher, meshgen
+    m, dyn, c, f, n = _case(meshgen.cavity(n=21))
+    ref = Environment(c, f, n, kernel=kernel)
+    ref.init()
+    ref.step(70)
+    env = Environment(c, f, n, kernel=kernel)
+    env.init()
+    env.step(30)
+    m.to_pickle(env, str(tmp_path / "ck"))
+    env.close()
+    env2, m2 = Mesher.from_pickle(str(tmp_path / "ck"))
+    assert env2.handle is None
+    env2.step(40)
+    for a, b in ((ref.cells.pdf, env2.cells.pdf), (ref.cells.rho, env2.cells.rho), (ref.nodes.pdf, env2.nodes.pdf),
+                 (ref.nodes.rho, env2.nodes.rho), (ref.faces.pdf, env2.faces.pdf)):
+        assert np.array_equal(np.asarray(a), np.asarray(b))

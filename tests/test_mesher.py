@@ -56,3 +56,18 @@ def test_cavity_config_sizes():
     assert raw.elements.shape == (3200, 3)
     assert raw.faces.shape == (4880, 2)
     assert raw.points.shape == (1681, 2)
+
+
+def test_pickle_round_trip_without_device(tmp_path):
+    """Checkpoint files hold the containers and the mesher; no GPU needed
+    until the environment steps."""
+    import numpy as np
+    from fvdbm_jax_gb300 import D2Q9, Environment, Mesher, meshgen
+    m = Mesher().import_meshpy(meshgen.cavity(9))
+    m.calc_mesh_properties()
+    c, f, n = m.to_env(D2Q9(0.6, 0.01), "upwind")
+    env = Environment(c, f, n)
+    m.to_pickle(env, str(tmp_path / "ck"))
+    env2, m2 = Mesher.from_pickle(str(tmp_path / "ck"))
+    assert np.array_equal(np.asarray(env2.cells.pdf), np.asarray(c.pdf))
+    assert np.array_equal(m2.points, m.points)
