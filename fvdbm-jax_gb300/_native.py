@@ -41,6 +41,7 @@ class Params(C.Structure):
         ("inv_tau", C.c_float), ("delta_t", C.c_float),
         ("c2", C.c_float), ("c4x2", C.c_float), ("c2x2", C.c_float),
         ("ordering", C.c_int32), ("kernel", C.c_int32), ("device", C.c_int32),
+        ("lattice", C.c_int32), ("c6x2", C.c_float),
     ]
 
 
@@ -123,7 +124,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_const_div_check.argtypes = [C.c_int32, C.c_float, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
     for name in EXPORTS:
         getattr(L, name)
-    if L.fvdbm_abi_version() != 2:
+    if L.fvdbm_abi_version() != 3:
         raise RuntimeError("libfvdbm ABI version mismatch")
     _LIB = L
     return L

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .dynamics import D2Q9
+from .dynamics import D2Q9, as_lattice
 
 F32, I32 = np.float32, np.int32
 
@@ -121,8 +121,8 @@ def from_any(cells, faces, nodes, dynamics=None):
     dyn = dynamics or getattr(cells, "dynamics", None)
     if dyn is None:
         raise ValueError("containers carry no dynamics; pass dynamics=")
-    if not isinstance(dyn, D2Q9):
-        dyn = D2Q9(dyn.tau, dyn.delta_t)
+    dyn = as_lattice(dyn)
+    Q = dyn.NUM_QUIVERS
     N = int(np.shape(cells.pdf)[0])
     F = int(np.shape(faces.pdf)[0])
     P = int(np.shape(nodes.pdf)[0])
@@ -130,7 +130,7 @@ def from_any(cells, faces, nodes, dynamics=None):
     c.pdf = _arr(cells.pdf, F32)
     c.rho = _arr(cells.rho, F32).reshape(N, 1)
     c.vel = _arr(cells.vel, F32).reshape(N, 2)
-    c.pdf_eq = _arr(cells.pdf_eq, F32).reshape(N, 9)
+    c.pdf_eq = _arr(cells.pdf_eq, F32).reshape(N, Q)
     c.face_indices = _arr(cells.face_indices, I32).reshape(N, -1)
     c.face_normals = _arr(cells.face_normals, I32).reshape(N, -1)
     for extra in ("centroids", "areas"):

@@ -164,10 +164,11 @@ int dalloc(Handle* h, T** out, size_t n, const std::vector<T>* init = nullptr) {
 int upload_nodes(Handle* h) {
   const HostPlan& hp = h->hp;
   if (hp.M == 0) return FVDBM_OK;
-  std::vector<float> pdf(size_t(Q) * hp.Mp, 0.0f), rho(hp.Mp, 0.0f), vel(size_t(2) * hp.Mp, 0.0f);
+  const int Qh = hp.q;
+  std::vector<float> pdf(size_t(Qh) * hp.Mp, 0.0f), rho(hp.Mp, 0.0f), vel(size_t(2) * hp.Mp, 0.0f);
   for (int d = 0; d < hp.M; ++d) {
     const int p = hp.node_orig[d];
-    for (int q = 0; q < Q; ++q) pdf[size_t(q) * hp.Mp + d] = h->node_pdf[size_t(p) * Q + q];
+    for (int q = 0; q < Qh; ++q) pdf[size_t(q) * hp.Mp + d] = h->node_pdf[size_t(p) * Qh + q];
     rho[d] = h->node_rho[p];
     vel[d] = h->node_vel[size_t(p) * 2];
     vel[hp.Mp + d] = h->node_vel[size_t(p) * 2 + 1];
@@ -223,7 +224,9 @@ int enqueue_steps(Handle* h, int n) {
   for (int s = 0; s < n; ++s) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
-    if (h->fnodes) {
+    if (h->hp.q == 13) {
+      CK(launch13_step(h->dp, fin, h->flux, fout, h->stream));
+    } else if (h->fnodes) {
       CK(launch_fused_nodes(with_nodes(h, h->node_cur, h->node_cur ^ 1), fin, fout, h->stream, /*pdl=*/true));
       h->node_last = h->node_cur;
       h->node_cur ^= 1;
@@ -392,6 +395,14 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   }
   h->fnodes = params->kernel == FVDBM_KERNEL_FUSED_NODES ||
               (auto_family && hp.fusable && hp.K == 3 && hp.stencil_first);
+  if (hp.q == 13) {
+    // D2Q13 runs on the staged kernels (d2q13.cu)
+    if (segs || (params->kernel != FVDBM_KERNEL_AUTO && params->kernel != FVDBM_KERNEL_STAGED)) {
+      h->err = "D2Q13 runs on the staged kernels only (FVDBM_KERNEL_AUTO or FVDBM_KERNEL_STAGED), not in a batch";
+      return create_fail(h, FVDBM_EINVAL);
+    }
+    h->fused = h->fnodes = false;
+  }
   const bool want_tile = params->kernel == FVDBM_KERNEL_TILE || params->kernel == FVDBM_KERNEL_TILE_SPLIT;
   if ((params->kernel == FVDBM_KERNEL_FUSED || want_tile) && !hp.fusable) {
     h->err = "the fused kernels need every cell face slot to name a face of that cell "
@@ -414,6 +425,7 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     return create_fail(h, FVDBM_EINVAL);
   }
   h->one = one_possible && params->kernel == FVDBM_KERNEL_ONE;
+  if (hp.q == 13) h->tile = h->one = false;
   if (segs) {
     if (!(hp.fusable && hp.K == 3)) {
       h->err = "a batch needs triangles (3 face slots per cell), every cell face slot naming a face of "
@@ -441,10 +453,14 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   p.c2 = params->c2;
   p.c4x2 = params->c4x2;
   p.c2x2 = params->c2x2;
+  p.c6x2 = params->c6x2;
+  p.q = hp.q;
   p.finite_n = hp.finite_n ? 1 : 0;
-  CR(make_cdiv(h->device, p.c2, h->stream, &p.d_c2));
-  CR(make_cdiv(h->device, p.c4x2, h->stream, &p.d_c4x2));
-  CR(make_cdiv(h->device, p.c2x2, h->stream, &p.d_c2x2));
+  if (hp.q == 9) {  // (the D2Q13 kernels divide with '/')
+    CR(make_cdiv(h->device, p.c2, h->stream, &p.d_c2));
+    CR(make_cdiv(h->device, p.c4x2, h->stream, &p.d_c4x2));
+    CR(make_cdiv(h->device, p.c2x2, h->stream, &p.d_c2x2));
+  }
 
 #define UP(field, vec)                                                        \
   do {                                                                        \
@@ -527,7 +543,7 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     if ((rc = dalloc(h, &h->d_area, hp.area.size(), &hp.area)) != FVDBM_OK) return create_fail(h, rc);
   {
     float* d = nullptr;
-    if ((rc = dalloc<float>(h, &d, size_t(Q) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
+    if ((rc = dalloc<float>(h, &d, size_t(hp.q) * hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
     p.node_pdf = d;
     if ((rc = dalloc<float>(h, &d, hp.Mp)) != FVDBM_OK) return create_fail(h, rc);
     p.node_rho = d;
@@ -537,17 +553,17 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     h->nbuf[0][1] = p.node_rho;
     h->nbuf[0][2] = p.node_vel;
     if (h->fnodes) {
-      const size_t sz[3] = {size_t(Q) * hp.Mp, size_t(hp.Mp), size_t(2) * hp.Mp};
+      const size_t sz[3] = {size_t(hp.q) * hp.Mp, size_t(hp.Mp), size_t(2) * hp.Mp};
       for (int k = 0; k < 3; ++k)
         if ((rc = dalloc<float>(h, &h->nbuf[1][k], sz[k])) != FVDBM_OK) return create_fail(h, rc);
     }
   }
   for (int b = 0; b < 2; ++b) {
-    if ((rc = dalloc<float>(h, &h->f[b], size_t(Q) * hp.Np)) != FVDBM_OK) return create_fail(h, rc);
-    CR(cudaMemsetAsync(h->f[b], 0, size_t(Q) * hp.Np * 4, h->stream));
+    if ((rc = dalloc<float>(h, &h->f[b], size_t(hp.q) * hp.Np)) != FVDBM_OK) return create_fail(h, rc);
+    CR(cudaMemsetAsync(h->f[b], 0, size_t(hp.q) * hp.Np * 4, h->stream));
   }
   if (!h->fused && !h->batch)
-    if ((rc = dalloc<float>(h, &h->flux, size_t(Q) * hp.Fp)) != FVDBM_OK) return create_fail(h, rc);
+    if ((rc = dalloc<float>(h, &h->flux, size_t(hp.q) * hp.Fp)) != FVDBM_OK) return create_fail(h, rc);
   if (h->batch) {
     const std::vector<float> it(case_inv_tau, case_inv_tau + hp.S), dt(case_dt, case_dt + hp.S);
     h->case_dt_host = dt;
@@ -572,25 +588,32 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     if ((rc = dalloc(h, &h->d_chunk_start, cs.size(), &cs)) != FVDBM_OK) return create_fail(h, rc);
     if ((rc = dalloc(h, &h->d_case_chunk, cc.size(), &cc)) != FVDBM_OK) return create_fail(h, rc);
   }
-  if ((rc = dalloc<float>(h, &h->stage, size_t(Q) * std::max(hp.N, hp.F))) != FVDBM_OK)
+  if ((rc = dalloc<float>(h, &h->stage, size_t(hp.q) * std::max(hp.N, hp.F))) != FVDBM_OK)
     return create_fail(h, rc);
   if ((rc = dalloc(h, &h->d_cell_new, hp.cell_new.size(), &hp.cell_new)) != FVDBM_OK)
     return create_fail(h, rc);
 
   // rest state: every pdf = feq(1, 0) = W (src/containers.py:29)
-  const float W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 9.0),
-                      (float)(1.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 36.0),
-                      (float)(1.0 / 36.0), (float)(1.0 / 36.0), (float)(1.0 / 36.0)};
-  h->node_pdf.resize(size_t(Q) * hp.P);
+  // (D2Q13: src/dynamics.py:96)
+  const float W9[9] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 9.0),
+                       (float)(1.0 / 9.0),  (float)(1.0 / 9.0),  (float)(1.0 / 36.0),
+                       (float)(1.0 / 36.0), (float)(1.0 / 36.0), (float)(1.0 / 36.0)};
+  const float W13[13] = {(float)(3.0 / 8.0),  (float)(1.0 / 12.0), (float)(1.0 / 12.0), (float)(1.0 / 12.0),
+                         (float)(1.0 / 12.0), (float)(1.0 / 16.0), (float)(1.0 / 16.0), (float)(1.0 / 16.0),
+                         (float)(1.0 / 16.0), (float)(1.0 / 96.0), (float)(1.0 / 96.0), (float)(1.0 / 96.0),
+                         (float)(1.0 / 96.0)};
+  const float* W = hp.q == 13 ? W13 : W9;
+  const int Qh = hp.q;
+  h->node_pdf.resize(size_t(Qh) * hp.P);
   for (int pp = 0; pp < hp.P; ++pp)
-    for (int q = 0; q < Q; ++q) h->node_pdf[size_t(pp) * Q + q] = W[q];
+    for (int q = 0; q < Qh; ++q) h->node_pdf[size_t(pp) * Qh + q] = W[q];
   h->node_rho.assign(hp.P, 0.0f);
   h->node_vel.assign(size_t(2) * hp.P, 0.0f);
   if ((rc = upload_nodes(h)) != FVDBM_OK) return create_fail(h, rc);
   {
-    std::vector<float> cells(size_t(Q) * hp.N);
+    std::vector<float> cells(size_t(Qh) * hp.N);
     for (int c = 0; c < hp.N; ++c)
-      for (int q = 0; q < Q; ++q) cells[size_t(c) * Q + q] = W[q];
+      for (int q = 0; q < Qh; ++q) cells[size_t(c) * Qh + q] = W[q];
     if ((rc = fvdbm_set_state(h, cells.data(), nullptr, nullptr, nullptr)) != FVDBM_OK)
       return create_fail(h, rc);
   }
@@ -768,8 +791,8 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
   if (cell_pdf && hp.N > 0) {
-    CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(Q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
-    CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream));
+    CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(hp.q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream, hp.q));
     if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
     // a retired batch case keeps its state in both buffers
     for (size_t s = 0; s < h->active.size(); ++s)
@@ -779,7 +802,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
     h->nodes_ready = false;
   }
   if (node_pdf || node_rho || node_vel) {
-    if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(Q) * hp.P * 4);
+    if (node_pdf) std::memcpy(h->node_pdf.data(), node_pdf, size_t(hp.q) * hp.P * 4);
     if (node_rho) std::memcpy(h->node_rho.data(), node_rho, size_t(hp.P) * 4);
     if (node_vel) std::memcpy(h->node_vel.data(), node_vel, size_t(2) * hp.P * 4);
     int rc = upload_nodes(h);
@@ -791,6 +814,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
 int fvdbm_set_cells_eq(void* handle, const float* rho, const float* vel) {
   if (!handle || !rho || !vel) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  if (h->hp.q != 9) return fail(h, FVDBM_EINVAL, "fvdbm_set_cells_eq supports D2Q9");
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
   if (hp.N == 0) return FVDBM_OK;
@@ -860,6 +884,14 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   CK(cudaSetDevice(h->device));
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
+  if (h->hp.q == 13) {  // nodes, faces and cells in phase 2
+    if (phase == 1) return FVDBM_OK;
+    if (phase != 2) return fail(h, FVDBM_EINVAL, "phase must be 1 or 2");
+    CK(launch13_step(h->dp, fin, h->flux, fout, h->stream));
+    h->cur ^= 1;
+    h->steps_done += 1;
+    return FVDBM_OK;
+  }
   if (h->fnodes) {
     // one launch per step: phase 1 only brings the nodes up to date
     if (phase == 1) return ensure_nodes(h);
@@ -914,24 +946,27 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
   CK(cudaSetDevice(h->device));
   const int N = hp.N;
   if (pdf && N > 0) {
-    CK(launch_gather_cells(h->f[h->cur], h->stage, h->d_cell_new, N, h->stream));
-    CK(cudaMemcpyAsync(pdf, h->stage, size_t(Q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(launch_gather_cells(h->f[h->cur], h->stage, h->d_cell_new, N, h->stream, hp.q));
+    CK(cudaMemcpyAsync(pdf, h->stage, size_t(hp.q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
   }
   if ((rho || vel || pdf_eq) && N > 0) {
     if (h->steps_done == 0) {
       if (rho) std::memset(rho, 0, size_t(N) * 4);
       if (vel) std::memset(vel, 0, size_t(2) * N * 4);
-      if (pdf_eq) std::memset(pdf_eq, 0, size_t(Q) * N * 4);
+      if (pdf_eq) std::memset(pdf_eq, 0, size_t(hp.q) * N * 4);
     } else {
       if (!h->mac) {
-        int rc = dalloc<float>(h, &h->mac, size_t(12) * hp.Np);
+        int rc = dalloc<float>(h, &h->mac, size_t(3 + hp.q) * hp.Np);
         if (rc != FVDBM_OK) return rc;
       }
       float* mr = h->mac;
       float* mv = h->mac + hp.Np;
       float* me = h->mac + size_t(3) * hp.Np;
-      CK(launch_macros(h->dp, h->f[h->cur ^ 1], mr, mv, me, h->stream));
+      if (hp.q == 13)
+        CK(launch13_macros(h->dp, h->f[h->cur ^ 1], mr, mv, me, h->stream));
+      else
+        CK(launch_macros(h->dp, h->f[h->cur ^ 1], mr, mv, me, h->stream));
       if (rho) {
         CK(launch_soa_to_aos(mr, h->stage, h->d_cell_new, N, hp.Np, 1, h->stream));
         CK(cudaMemcpyAsync(rho, h->stage, size_t(N) * 4, cudaMemcpyDeviceToHost, h->stream));
@@ -943,8 +978,8 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
         CK(cudaStreamSynchronize(h->stream));
       }
       if (pdf_eq) {
-        CK(launch_gather_cells(me, h->stage, h->d_cell_new, N, h->stream));
-        CK(cudaMemcpyAsync(pdf_eq, h->stage, size_t(Q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(launch_gather_cells(me, h->stage, h->d_cell_new, N, h->stream, hp.q));
+        CK(cudaMemcpyAsync(pdf_eq, h->stage, size_t(hp.q) * N * 4, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
       }
     }
@@ -959,7 +994,7 @@ int fvdbm_get_nodes(void* handle, float* pdf, float* rho, float* vel) {
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
   if (hp.M > 0) {
-    std::vector<float> dp(size_t(Q) * hp.Mp), dr(hp.Mp), dv(size_t(2) * hp.Mp);
+    std::vector<float> dp(size_t(hp.q) * hp.Mp), dr(hp.Mp), dv(size_t(2) * hp.Mp);
     const DevPlan q = h->fnodes ? with_nodes(h, h->node_last, h->node_last) : h->dp;
     CK(cudaMemcpyAsync(dp.data(), q.node_pdf, dp.size() * 4, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(dr.data(), q.node_rho, dr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
@@ -967,13 +1002,13 @@ int fvdbm_get_nodes(void* handle, float* pdf, float* rho, float* vel) {
     CK(cudaStreamSynchronize(h->stream));
     for (int d = 0; d < hp.M; ++d) {
       const int p = hp.node_orig[d];
-      for (int q = 0; q < Q; ++q) h->node_pdf[size_t(p) * Q + q] = dp[size_t(q) * hp.Mp + d];
+      for (int q = 0; q < hp.q; ++q) h->node_pdf[size_t(p) * hp.q + q] = dp[size_t(q) * hp.Mp + d];
       h->node_rho[p] = dr[d];
       h->node_vel[size_t(p) * 2] = dv[d];
       h->node_vel[size_t(p) * 2 + 1] = dv[hp.Mp + d];
     }
   }
-  if (pdf) std::memcpy(pdf, h->node_pdf.data(), size_t(Q) * hp.P * 4);
+  if (pdf) std::memcpy(pdf, h->node_pdf.data(), size_t(hp.q) * hp.P * 4);
   if (rho) std::memcpy(rho, h->node_rho.data(), size_t(hp.P) * 4);
   if (vel) std::memcpy(vel, h->node_vel.data(), size_t(2) * hp.P * 4);
   return FVDBM_OK;
@@ -986,17 +1021,20 @@ int fvdbm_get_face_fluxes(void* handle, float* flux) {
   CK(cudaSetDevice(h->device));
   if (hp.F == 0) return FVDBM_OK;
   if (!h->flux) {
-    int rc = dalloc<float>(h, &h->flux, size_t(Q) * hp.Fp);
+    int rc = dalloc<float>(h, &h->flux, size_t(hp.q) * hp.Fp);
     if (rc != FVDBM_OK) return rc;
   }
-  CK(launch_face_flux(h->fnodes ? with_nodes(h, h->node_last, h->node_last) : h->dp, h->f[h->cur ^ 1], h->flux,
-                      h->stream));
-  std::vector<float> soa(size_t(Q) * hp.Fp);
+  if (hp.q == 13)
+    CK(launch13_face_flux(h->dp, h->f[h->cur ^ 1], h->flux, h->stream));
+  else
+    CK(launch_face_flux(h->fnodes ? with_nodes(h, h->node_last, h->node_last) : h->dp, h->f[h->cur ^ 1], h->flux,
+                        h->stream));
+  std::vector<float> soa(size_t(hp.q) * hp.Fp);
   CK(cudaMemcpyAsync(soa.data(), h->flux, soa.size() * 4, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int j = 0; j < hp.F; ++j) {
     const int f = hp.face_old[j];
-    for (int q = 0; q < Q; ++q) flux[size_t(f) * Q + q] = soa[size_t(q) * hp.Fp + j];
+    for (int q = 0; q < hp.q; ++q) flux[size_t(f) * hp.q + q] = soa[size_t(q) * hp.Fp + j];
   }
   return FVDBM_OK;
 }
@@ -1004,6 +1042,7 @@ int fvdbm_get_face_fluxes(void* handle, float* flux) {
 int fvdbm_residual(void* handle, double* res_u, double* mass) {
   if (!handle || !res_u || !mass) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  if (h->hp.q != 9) return fail(h, FVDBM_EINVAL, "the convergence monitor supports D2Q9");
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
   const int nb = residual_chunks(hp.N, kResidualChunk);
@@ -1129,6 +1168,7 @@ extern "C" int fvdbm_step_static_scratch(void* handle, int32_t n_steps) {
     return fail(h, FVDBM_EINVAL,
                 "fvdbm_step_static_scratch steps the staged kernels only: create the handle with "
                 "FVDBM_KERNEL_STAGED");
+  if (hp.q != 9) return fail(h, FVDBM_EINVAL, "fvdbm_step_static_scratch steps D2Q9 meshes only");
   if (hp.Fp > FVDBM_STATIC_SCRATCH_MAX_FACES)
     return fail(h, FVDBM_EINVAL,
                 "fvdbm_step_static_scratch: the mesh has " + std::to_string(hp.F) + " faces (" +

@@ -1,0 +1,244 @@
+// D2Q13 lattice (src/dynamics.py:77-102): the staged step (boundary nodes,
+// per-face fluxes, per-cell gather and update) and the read-back helpers
+// with 13 velocities, including the (+-2, 0), (0, +-2) ones, and the
+// third-order equilibrium
+//   feq_q = (W_q rho) * (((((1 + a/C^2) + a^2/(2C^4)) - u.u/(2C^2))
+//                          + a^3/(2C^6)) - 3 a u.u/(2C^4)),   a = xi_q . u,
+// evaluated in that order with a^3 = a*(a*a) (jax's integer_pow), so that
+// results equal the reference's float32 step bit for bit.  The float32
+// lattice constants come from the host (C = 1/sqrt(2) in float32).
+//
+// Layouts as the D2Q9 kernels: cell pdfs AoSoA [Np/32][13][32], face fluxes
+// [13][Fp], node state [13][Mp] / [Mp] / [2][Mp].
+#include "fvdbm_internal.h"
+
+namespace fvdbm {
+
+namespace {
+
+constexpr int Q13 = 13;
+__constant__ float c_kx13[Q13] = {0, 1, 0, -1, 0, 1, -1, -1, 1, 2, 0, -2, 0};
+__constant__ float c_ky13[Q13] = {0, 0, 1, 0, -1, 1, 1, -1, -1, 0, 2, 0, -2};
+__constant__ float c_w13[Q13] = {(float)(3.0 / 8.0),   (float)(1.0 / 12.0), (float)(1.0 / 12.0),
+                                 (float)(1.0 / 12.0),  (float)(1.0 / 12.0), (float)(1.0 / 16.0),
+                                 (float)(1.0 / 16.0),  (float)(1.0 / 16.0), (float)(1.0 / 16.0),
+                                 (float)(1.0 / 96.0),  (float)(1.0 / 96.0), (float)(1.0 / 96.0),
+                                 (float)(1.0 / 96.0)};
+
+__device__ __forceinline__ size_t base13(int c) { return size_t(c >> 5) * (Q13 * 32) + size_t(c & 31); }
+
+__device__ __forceinline__ void load13(const float* __restrict__ f, int c, float out[Q13]) {
+  const float* b = f + base13(c);
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) out[q] = __ldg(b + q * 32);
+}
+
+// rho = sum_q f_q; u = (xi^T f)/rho, every product xi_q f_q kept in the fold
+// (src/dynamics.py:35-47)
+__device__ __forceinline__ void macros13(const float f[Q13], float& rho, float& ux, float& uy) {
+  float r = f[0], mx = c_kx13[0] * f[0], my = c_ky13[0] * f[0];
+#pragma unroll
+  for (int q = 1; q < Q13; ++q) {
+    r = r + f[q];
+    mx = mx + c_kx13[q] * f[q];
+    my = my + c_ky13[q] * f[q];
+  }
+  rho = r;
+  ux = mx / r;
+  uy = my / r;
+}
+
+__device__ __forceinline__ void feq13(float rho, float ux, float uy, const DevPlan& p, float out[Q13]) {
+  const float uu = ux * ux + uy * uy;
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) {
+    const float a = c_kx13[q] * ux + c_ky13[q] * uy;
+    float s = 1.0f + a / p.c2;
+    s = s + (a * a) / p.c4x2;
+    s = s - uu / p.c2x2;
+    s = s + (a * (a * a)) / p.c6x2;
+    s = s - ((3.0f * a) * uu) / p.c4x2;
+    out[q] = (c_w13[q] * rho) * s;
+  }
+}
+
+// Boundary nodes (src/containers.py:339-404, utils/utils.py:34-60), one
+// thread per computed node, its stencil entries folded in order.
+__global__ void k13_nodes(DevPlan p, const float* __restrict__ f) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= p.Mc) return;
+  const int type = p.nd_type[m];
+  const int e0 = p.nd_ptr[m], e1 = p.nd_ptr[m + 1];
+  float ar = 0.0f, ax = 0.0f, ay = 0.0f, an[Q13];
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) an[q] = 0.0f;
+  for (int e = e0; e < e1; ++e) {
+    const unsigned code = p.nd_cell[e];
+    const float w = p.nd_w[e];
+    float fc[Q13], eq[Q13];
+    load13(f, int(code & ~ND_NEQ_ZERO), fc);
+    float rho, ux, uy;
+    macros13(fc, rho, ux, uy);
+    feq13(rho, ux, uy, p, eq);
+    const bool zero = (code & ND_NEQ_ZERO) != 0;
+    const bool first = e == e0;
+    ar = first ? rho * w : ar + rho * w;
+    ax = first ? ux * w : ax + ux * w;
+    ay = first ? uy * w : ay + uy * w;
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) {
+      const float x = (zero ? 0.0f : fc[q] - eq[q]) * w;
+      an[q] = first ? x : an[q] + x;
+    }
+  }
+  if (p.nd_npad[m] > 0) {
+    // padded (-1, weight 0) entries gather the last cell
+    float fc[Q13];
+    load13(f, p.last_cell, fc);
+    float rho, ux, uy;
+    macros13(fc, rho, ux, uy);
+    const bool none = e1 == e0;
+    ar = none ? rho * 0.0f : ar + rho * 0.0f;
+    ax = none ? ux * 0.0f : ax + ux * 0.0f;
+    ay = none ? uy * 0.0f : ay + uy * 0.0f;
+  }
+  const float sw = p.nd_sumw[m];
+  float rho_p, ux_p, uy_p;
+  if (type == 1) {
+    rho_p = ar / sw;
+    ux_p = p.node_vel[m];
+    uy_p = p.node_vel[p.Mp + m];
+    p.node_rho[m] = rho_p;
+  } else {
+    rho_p = p.node_rho[m];
+    ux_p = ax / sw;
+    uy_p = ay / sw;
+    p.node_vel[m] = ux_p;
+    p.node_vel[p.Mp + m] = uy_p;
+  }
+  float eqn[Q13];
+  feq13(rho_p, ux_p, uy_p, p, eqn);
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) p.node_pdf[size_t(q) * p.Mp + m] = eqn[q] + an[q] / sw;
+}
+
+// Face fluxes (src/containers.py:191-287), one thread per face.
+__global__ void k13_face(DevPlan p, const float* __restrict__ f, float* __restrict__ flux) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.F) return;
+  const int s0 = p.fs0[j], s1 = p.fs1[j];
+  float lf[Q13], rf[Q13];
+  if (s0 >= 0 && s1 >= 0) {
+    load13(f, s0, lf);
+    load13(f, s1, rf);
+  } else {
+    const int a = p.fna[j], b = p.fnb[j];
+    float mq[Q13];
+#pragma unroll
+    for (int q = 0; q < Q13; ++q)
+      mq[q] = (p.node_pdf[size_t(q) * p.Mp + a] + p.node_pdf[size_t(q) * p.Mp + b]) / 2.0f;
+    if (s0 >= 0) {
+      load13(f, s0, lf);
+    } else {
+      float kf[Q13];
+      load13(f, p.fkl[j], kf);
+#pragma unroll
+      for (int q = 0; q < Q13; ++q) lf[q] = mq[q] + (mq[q] - kf[q]) * p.frl[j];
+    }
+    if (s1 >= 0) {
+      load13(f, s1, rf);
+    } else {
+      float kf[Q13];
+      load13(f, p.fkr[j], kf);
+#pragma unroll
+      for (int q = 0; q < Q13; ++q) rf[q] = mq[q] + (mq[q] - kf[q]) * p.frr[j];
+    }
+  }
+  const float nx = p.fnx[j], ny = p.fny[j], L = p.fL[j];
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) {
+    const float v = c_kx13[q] * nx + c_ky13[q] * ny;
+    float phi;
+    if (p.scheme == 0) {
+      phi = v >= 0.0f ? lf[q] : rf[q];
+    } else {
+      const float w = p.fr[j] - (v * p.dt) / p.fD2[j];
+      phi = lf[q] + (rf[q] - lf[q]) * w;
+    }
+    flux[size_t(q) * p.Fp + j] = (phi * v) * L;
+  }
+}
+
+// Cell update (src/containers.py:107-121), one thread per cell.
+__global__ void k13_gather(DevPlan p, const float* __restrict__ fin, const float* __restrict__ flux,
+                           float* __restrict__ fout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  const size_t Np = p.Np;
+  float f[Q13], eq[Q13], acc[Q13];
+  load13(fin, i, f);
+  float rho, ux, uy;
+  macros13(f, rho, ux, uy);
+  feq13(rho, ux, uy, p, eq);
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) acc[q] = 0.0f;
+  for (int k = 0; k < p.K; ++k) {
+    const int fi = p.cf_face[k * Np + i];
+    const float sg = p.cf_sign[k * Np + i];
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) {
+      const float x = flux[size_t(q) * p.Fp + fi] * sg;
+      acc[q] = (k == 0) ? x : acc[q] + x;
+    }
+  }
+  if (p.fv) {
+    const float ia = p.inv_area[i];
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) acc[q] = acc[q] * ia;
+  }
+  float* o = fout + base13(i);
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+}
+
+// rho [Np], vel [2][Np], feq AoSoA of a pdf buffer (read-back)
+__global__ void k13_macros(DevPlan p, const float* __restrict__ f, float* __restrict__ rho_o,
+                           float* __restrict__ vel_o, float* __restrict__ feq_o) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  float fc[Q13], eq[Q13];
+  load13(f, i, fc);
+  float rho, ux, uy;
+  macros13(fc, rho, ux, uy);
+  feq13(rho, ux, uy, p, eq);
+  rho_o[i] = rho;
+  vel_o[i] = ux;
+  vel_o[size_t(p.Np) + i] = uy;
+  float* o = feq_o + base13(i);
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) o[q * 32] = eq[q];
+}
+
+inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
+
+}  // namespace
+
+cudaError_t launch13_step(const DevPlan& p, const float* fin, float* flux, float* fout, cudaStream_t s) {
+  if (p.Mc > 0) k13_nodes<<<nblk(p.Mc, 128), 128, 0, s>>>(p, fin);
+  if (p.F > 0) k13_face<<<nblk(p.F, 256), 256, 0, s>>>(p, fin, flux);
+  if (p.N > 0) k13_gather<<<nblk(p.N, 256), 256, 0, s>>>(p, fin, flux, fout);
+  return cudaGetLastError();
+}
+
+cudaError_t launch13_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s) {
+  if (p.F > 0) k13_face<<<nblk(p.F, 256), 256, 0, s>>>(p, f, flux);
+  return cudaGetLastError();
+}
+
+cudaError_t launch13_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
+                            cudaStream_t s) {
+  if (p.N > 0) k13_macros<<<nblk(p.N, 256), 256, 0, s>>>(p, f, rho, vel, feq);
+  return cudaGetLastError();
+}
+
+}  // namespace fvdbm

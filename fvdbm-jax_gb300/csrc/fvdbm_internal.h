@@ -55,6 +55,7 @@ struct HostPlan {
   int Np = 0;  // padded row stride of [9][Np] cell arrays
   int Fp = 0;  // padded row stride of [9][Fp] face arrays
   int scheme = 0, variant = 0;
+  int q = 9;  // lattice velocities
   bool fv = false;
   bool fusable = false;
   int ordering = 0;
@@ -168,6 +169,8 @@ struct DevPlan {
   int last_cell;
   int finite_n;  // every face normal is finite (enables the symmetric xi.n form)
   float inv_tau, dt, c2, c4x2, c2x2;
+  float c6x2;  // D2Q13: 2 C^6
+  int q;       // lattice velocities: 9 or 13
   CDiv d_c2, d_c4x2, d_c2x2;
   // staged faces
   const int* fs0;
@@ -298,11 +301,16 @@ cudaError_t launch_copy_cells(const float* src, float* dst, int c0, int c1, cuda
 // *bad must be zeroed and *example set to 0xFFFFFFFF.
 cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsigned* example,
                               cudaStream_t s);
-// [N][9] reference order <-> AoSoA device order (cell_new: reference -> device)
+// [N][q] reference order <-> AoSoA device order (cell_new: reference -> device)
 cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* cell_new, int N,
-                                 cudaStream_t s);
+                                 cudaStream_t s, int q = Q);
 cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
-                                cudaStream_t s);
+                                cudaStream_t s, int q = Q);
+// D2Q13 (d2q13.cu): the staged step, the face fluxes alone, read-back macros
+cudaError_t launch13_step(const DevPlan& p, const float* fin, float* flux, float* fout, cudaStream_t s);
+cudaError_t launch13_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);
+cudaError_t launch13_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
+                            cudaStream_t s);
 // SoA [rows][Np] device order -> [N][rows] reference order
 cudaError_t launch_soa_to_aos(const float* src, float* dst, const int* cell_new, int N, int Np,
                               int rows, cudaStream_t s);

@@ -673,23 +673,25 @@ __global__ void __launch_bounds__(256) k_macros(DevPlan p, const float* __restri
 }
 
 // [N][9] reference order -> AoSoA device order.
+template <int QQ>
 __global__ void k_aos_to_cells(const float* __restrict__ src, float* __restrict__ dst,
                                const int* __restrict__ cell_new, int N) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= N) return;
-  float* o = dst + cell_base(cell_new[c], Q);
+  float* o = dst + cell_base(cell_new[c], QQ);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) o[q * 32] = src[size_t(c) * Q + q];
+  for (int q = 0; q < QQ; ++q) o[q * 32] = src[size_t(c) * QQ + q];
 }
 
-// AoSoA device order -> [N][9] reference order.
+// AoSoA device order -> [N][Q] reference order.
+template <int QQ>
 __global__ void k_cells_to_aos(const float* __restrict__ src, float* __restrict__ dst,
                                const int* __restrict__ cell_new, int N) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= N) return;
-  const float* b = src + cell_base(cell_new[c], Q);
+  const float* b = src + cell_base(cell_new[c], QQ);
 #pragma unroll
-  for (int q = 0; q < Q; ++q) dst[size_t(c) * Q + q] = b[q * 32];
+  for (int q = 0; q < QQ; ++q) dst[size_t(c) * QQ + q] = b[q * 32];
 }
 
 // SoA [rows][Np] device order -> [N][rows] reference order.
@@ -943,16 +945,22 @@ cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsign
 }
 
 cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* cell_new, int N,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, int q) {
   if (N == 0) return cudaSuccess;
-  k_aos_to_cells<<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
+  if (q == 13)
+    k_aos_to_cells<13><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
+  else
+    k_aos_to_cells<Q><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
-                                cudaStream_t s) {
+                                cudaStream_t s, int q) {
   if (N == 0) return cudaSuccess;
-  k_cells_to_aos<<<blocks(N, 256), 256, 0, s>>>(src, dst_aos, cell_new, N);
+  if (q == 13)
+    k_cells_to_aos<13><<<blocks(N, 256), 256, 0, s>>>(src, dst_aos, cell_new, N);
+  else
+    k_cells_to_aos<Q><<<blocks(N, 256), 256, 0, s>>>(src, dst_aos, cell_new, N);
   return cudaGetLastError();
 }
 

@@ -164,6 +164,9 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
   if (pr.flux_scheme != FVDBM_UPWIND && pr.flux_scheme != FVDBM_LAX_WENDROFF)
     return "Unknown flux scheme";
   if (pr.variant < 0 || pr.variant > 2) return "unknown flux variant";
+  hp.q = pr.lattice == 0 ? 9 : pr.lattice;
+  if (hp.q != 9 && hp.q != 13) return "lattice must be 9 (D2Q9) or 13 (D2Q13)";
+  if (hp.q == 13 && pr.variant != 0) return "D2Q13 takes no flux-scale variant";
   if (N > 0 && K > 0 && (!m.cell_face_indices || !m.cell_face_signs)) return "cell face arrays missing";
   if (F > 0 && (!m.face_cells || !m.face_dists || !m.face_nodes || !m.face_n || !m.face_L))
     return "face arrays missing";
@@ -688,8 +691,8 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
   // algorithmic bytes of one step: pdf read+write, cell->face slots, face
   // geometry (2 slot ints + n + L, + 2 distances for Lax-Wendroff) and the
   // boundary-node pdf write + read
-  hp.bytes_per_step = 72.0 * N + 4.0 * K * N + 20.0 * F +
-                      (pr.flux_scheme == FVDBM_LAX_WENDROFF ? 8.0 * F : 0.0) + 72.0 * hp.Mc;
+  hp.bytes_per_step = 8.0 * hp.q * N + 4.0 * K * N + 20.0 * F +
+                      (pr.flux_scheme == FVDBM_LAX_WENDROFF ? 8.0 * F : 0.0) + 8.0 * hp.q * hp.Mc;
   return "";
 }
 

@@ -1,5 +1,5 @@
-"""D2Q9 lattice (reference ``src/dynamics.py:50-74``) and the float32 scalars
-the kernels need.
+"""D2Q9 and D2Q13 lattices (reference ``src/dynamics.py:50-102``) and the
+float32 scalars the kernels need.
 
 The reference keeps every array in float32 (x64 is never enabled) and treats
 ``tau``/``delta_t`` as Python scalars, so:
@@ -48,6 +48,8 @@ class D2Q9:
     def c2x2(self) -> np.float32:
         return F32(F32(2) * F32(self.C * self.C))
 
+    c6x2 = F32(0)  # (third-order term of D2Q13 only)
+
     @property
     def inv_tau(self) -> np.float32:
         return F32(np.asarray(1 / self.tau).astype(F32))
@@ -76,3 +78,46 @@ class D2Q9:
 
     def __repr__(self) -> str:
         return f"D2Q9(tau={self.tau}, delta_t={self.delta_t})"
+
+
+class D2Q13(D2Q9):
+    """D2Q13 dynamics (reference ``D2Q13(tau, delta_t)``,
+    ``src/dynamics.py:77-102``): 13 velocities including (+-2, 0), (0, +-2),
+    C = 1/sqrt(2) in float32, and the third-order equilibrium
+    ``(W*rho) * ((((1 + a/C^2) + a^2/(2C^4)) - u.u/(2C^2)) + a^3/(2C^6) - 3 a u.u/(2C^4))``
+    with the powers of C and a formed as jax's integer_pow forms them
+    (C^4 = (C*C)*(C*C), C^6 = (C*C)*C^4, a^3 = a*(a*a))."""
+
+    NUM_QUIVERS = 13
+    KSI = np.array([[0, 0], [1, 0], [0, 1], [-1, 0], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1],
+                    [2, 0], [0, 2], [-2, 0], [0, -2]], dtype=np.int32)
+    W = np.array([3 / 8, 1 / 12, 1 / 12, 1 / 12, 1 / 12, 1 / 16, 1 / 16, 1 / 16, 1 / 16,
+                  1 / 96, 1 / 96, 1 / 96, 1 / 96], dtype=F32)
+    C = F32(1) / np.sqrt(F32(2))
+
+    @property
+    def c6x2(self) -> np.float32:
+        c2 = F32(self.C * self.C)
+        return F32(F32(2) * F32(c2 * F32(c2 * c2)))
+
+    def calc_eq(self, rho, vel) -> np.ndarray:
+        rho = np.asarray(rho, dtype=F32)
+        vel = np.asarray(vel, dtype=F32)
+        ksi = self.KSI.astype(F32)
+        a = ksi[:, 0] * vel[..., 0:1] + ksi[:, 1] * vel[..., 1:2]
+        uu = vel[..., 0:1] * vel[..., 0:1] + vel[..., 1:2] * vel[..., 1:2]
+        inner = ((((F32(1) + a / self.c2) + (a * a) / self.c4x2) - uu / self.c2x2)
+                 + (a * (a * a)) / self.c6x2) - ((F32(3) * a) * uu) / self.c4x2
+        return (self.W * rho) * inner
+
+    def __repr__(self) -> str:
+        return f"D2Q13(tau={self.tau}, delta_t={self.delta_t})"
+
+
+def as_lattice(dyn):
+    """This package's dynamics object for any dynamics with tau/delta_t
+    (the reference's D2Q9/D2Q13 or these), chosen by NUM_QUIVERS."""
+    if isinstance(dyn, D2Q9):
+        return dyn
+    cls = D2Q13 if int(getattr(dyn, "NUM_QUIVERS", 9)) == 13 else D2Q9
+    return cls(dyn.tau, dyn.delta_t)

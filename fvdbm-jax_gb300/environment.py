@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _native as nat
 from .containers import Cells, Faces, Nodes, _Container, from_any
-from .dynamics import D2Q9
+from .dynamics import D2Q9, as_lattice
 
 F32, I32 = np.float32, np.int32
 
@@ -62,9 +62,7 @@ def pack(c, f, n, *, ordering="auto", kernel="auto", device=0, finite_volume=Fal
     sizes (N, F, P) and the case's D2Q9 dynamics."""
     if f.flux_scheme not in ("upwind", "lax_wendroff"):
         raise ValueError(f"Unknown flux scheme: {f.flux_scheme}")
-    dyn = c.dynamics
-    if not isinstance(dyn, D2Q9):
-        dyn = D2Q9(dyn.tau, dyn.delta_t)
+    dyn = as_lattice(c.dynamics)
     a = {
         "cfi": np.ascontiguousarray(c.face_indices, I32),
         "cfs": np.ascontiguousarray(c.face_normals, I32),
@@ -105,7 +103,7 @@ def pack(c, f, n, *, ordering="auto", kernel="auto", device=0, finite_volume=Fal
     params = nat.Params(nat.FVDBM_UPWIND if f.flux_scheme == "upwind" else nat.FVDBM_LAX_WENDROFF,
                         variant, float(dyn.inv_tau), float(dyn.dt32), float(dyn.c2),
                         float(dyn.c4x2), float(dyn.c2x2), _ORDER[order], _KERNEL[kernel],
-                        int(device))
+                        int(device), int(dyn.NUM_QUIVERS), float(dyn.c6x2))
     return mesh, params, a, (N, F, P), dyn
 
 
@@ -159,6 +157,7 @@ class Environment:
             raise nat.FvdbmError(f"fvdbm_create failed ({rc}): {msg}")
         self._h = h
         self._dyn = dyn
+        self._Q = int(dyn.NUM_QUIVERS)
         self._N, self._F, self._P = N, F, P
         self._upload_all()
         for cont in (c, f, n):
@@ -272,7 +271,7 @@ class Environment:
         if cont is self.cells:
             N = self._N
             if name == "pdf":
-                out = np.empty((N, 9), F32)
+                out = np.empty((N, self._Q), F32)
                 nat.check(L.fvdbm_get_cells(self._h, nat.fptr(out), None, None, None), self._h)
             elif self._steps == 0:
                 return
@@ -283,16 +282,16 @@ class Environment:
                 out = np.empty((N, 2), F32)
                 nat.check(L.fvdbm_get_cells(self._h, None, None, nat.fptr(out), None), self._h)
             else:
-                out = np.empty((N, 9), F32)
+                out = np.empty((N, self._Q), F32)
                 nat.check(L.fvdbm_get_cells(self._h, None, None, None, nat.fptr(out)), self._h)
         elif cont is self.faces:
             if self._steps == 0:
                 return
-            out = np.empty((self._F, 9), F32)
+            out = np.empty((self._F, self._Q), F32)
             nat.check(L.fvdbm_get_face_fluxes(self._h, nat.fptr(out)), self._h)
         else:
             P = self._P
-            pdf, rho, vel = np.empty((P, 9), F32), np.empty((P, 1), F32), np.empty((P, 2), F32)
+            pdf, rho, vel = np.empty((P, self._Q), F32), np.empty((P, 1), F32), np.empty((P, 2), F32)
             nat.check(L.fvdbm_get_nodes(self._h, nat.fptr(pdf), nat.fptr(rho), nat.fptr(vel)), self._h)
             for k, v in (("pdf", pdf), ("rho", rho), ("vel", vel)):
                 object.__setattr__(cont, k, v)
@@ -306,8 +305,8 @@ class Environment:
         L = nat.lib()
         if cont is self.cells and name == "pdf":
             pdf = np.ascontiguousarray(object.__getattribute__(cont, "pdf"), F32)
-            if pdf.shape != (self._N, 9):
-                raise ValueError(f"cells.pdf must be [{self._N},9]")
+            if pdf.shape != (self._N, self._Q):
+                raise ValueError(f"cells.pdf must be [{self._N},{self._Q}]")
             nat.check(L.fvdbm_set_state(self._h, nat.fptr(pdf), None, None, None), self._h)
             self._version += 1
             self._fresh[(id(cont), "pdf")] = self._version

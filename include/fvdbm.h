@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FVDBM_ABI_VERSION 2
+#define FVDBM_ABI_VERSION 3
 
 #define FVDBM_OK 0
 #define FVDBM_EINVAL (-1)  /* invalid argument or inconsistent mesh */
@@ -106,6 +106,11 @@ typedef struct fvdbm_params {
   int32_t ordering;    /* FVDBM_ORDER_* */
   int32_t kernel;      /* FVDBM_KERNEL_* */
   int32_t device;      /* CUDA device ordinal */
+  int32_t lattice;     /* velocities: 9 (D2Q9, also when 0) or 13 (D2Q13,
+                          src/dynamics.py:77-102: staged kernels only, no
+                          flux-scale variant; c2, c4x2, c2x2 are then those of
+                          C = 1/sqrt(2)) */
+  float c6x2;          /* D2Q13: 2*C^6 with C^6 = (C*C)*((C*C)*(C*C)) */
 } fvdbm_params_t;
 
 /* Sizes and the algorithmic traffic of one step, for reporting. */

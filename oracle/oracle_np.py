@@ -45,6 +45,25 @@ C2 = F32(C * C)
 C4X2 = F32(F32(2) * F32(C2 * C2))
 C2X2 = F32(F32(2) * C2)
 
+# D2Q13 (src/dynamics.py:77-102): C = 1/sqrt(2); the powers of C as jax's
+# integer_pow forms them (C**4 = (C*C)*(C*C), C**6 = (C*C)*((C*C)*(C*C)))
+KSI13 = np.array([[0, 0], [1, 0], [0, 1], [-1, 0], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1],
+                  [2, 0], [0, 2], [-2, 0], [0, -2]], dtype=np.int32)
+KSI13_F = KSI13.astype(F32)
+W13 = np.array([3 / 8, 1 / 12, 1 / 12, 1 / 12, 1 / 12, 1 / 16, 1 / 16, 1 / 16, 1 / 16,
+                1 / 96, 1 / 96, 1 / 96, 1 / 96], dtype=F32)
+C13 = F32(1) / np.sqrt(F32(2))
+C13_2 = F32(C13 * C13)
+C13_4 = F32(C13_2 * C13_2)
+C13_4X2 = F32(F32(2) * C13_4)
+C13_2X2 = F32(F32(2) * C13_2)
+C13_6X2 = F32(F32(2) * F32(C13_2 * C13_4))
+
+
+def ksi(q: int) -> np.ndarray:
+    """Lattice velocities (float32) of the 9- or 13-velocity lattice."""
+    return KSI_F if q == 9 else KSI13_F
+
 
 def _fold(x: np.ndarray, axis: int) -> np.ndarray:
     x = np.moveaxis(x, axis, 0)
@@ -58,17 +77,24 @@ def calc_macro(pdf: np.ndarray):
     """rho = sum_q f_q (``src/dynamics.py:35-37``); u = (KSI^T f)/rho
     (``:39-41``).  pdf [M,9] -> rho [M,1], vel [M,2]."""
     rho = _fold(pdf, 1)[:, None]
-    num = _fold(KSI_F.T[None, :, :] * pdf[:, None, :], 2)      # [M,2]
+    K = ksi(pdf.shape[1])
+    num = _fold(K.T[None, :, :] * pdf[:, None, :], 2)          # [M,2]
     return rho, num / rho
 
 
-def calc_eq(rho: np.ndarray, vel: np.ndarray) -> np.ndarray:
-    """BGK equilibrium (``src/dynamics.py:70-74``): ``(W*rho)*(((1 + a/C^2)
-    + a^2/(2C^4)) - u.u/(2C^2))``, a = KSI.u folded over x then y."""
-    a = _fold(KSI_F[None, :, :] * vel[:, None, :], 2)           # [M,9]
+def calc_eq(rho: np.ndarray, vel: np.ndarray, q: int = 9) -> np.ndarray:
+    """Equilibrium.  D2Q9 (``src/dynamics.py:70-74``): ``(W*rho)*(((1 +
+    a/C^2) + a^2/(2C^4)) - u.u/(2C^2))``, a = KSI.u folded over x then y.
+    D2Q13 (``:97-98``) adds ``+ a^3/(2C^6) - 3 a u.u/(2C^4)`` in that order,
+    with a^3 = a*(a*a) as jax's integer_pow forms it."""
+    a = _fold(ksi(q)[None, :, :] * vel[:, None, :], 2)         # [M,Q]
     uu = _fold(vel * vel, 1)[:, None]                          # [M,1]
-    inner = ((1 + a / C2) + (a * a) / C4X2) - uu / C2X2
-    return (W * rho) * inner
+    if q == 9:
+        inner = ((1 + a / C2) + (a * a) / C4X2) - uu / C2X2
+        return (W * rho) * inner
+    a3 = a * (a * a)
+    inner = ((((1 + a / C13_2) + (a * a) / C13_4X2) - uu / C13_2X2) + a3 / C13_6X2) - ((3 * a) * uu) / C13_4X2
+    return (W13 * rho) * inner
 
 
 def _idw(x: np.ndarray, w: np.ndarray, sumw: np.ndarray) -> np.ndarray:
@@ -94,10 +120,11 @@ def node_pdfs(geo, cells_pdf, cells_eq, cells_rho, cells_vel, nodes_pdf, nodes_r
     neq_k = np.where((idx == -1)[:, :, None], F32(0), cells_pdf[idx] - cells_eq[idx])
     neq = _idw(neq_k.astype(F32), w, sumw)                     # [P,9]
 
+    q = cells_pdf.shape[1]
     rho = np.where(t == 1, rho_ext, nodes_rho).astype(F32)
-    pdf = np.where(t == 1, calc_eq(rho, nodes_vel) + neq, nodes_pdf).astype(F32)
+    pdf = np.where(t == 1, calc_eq(rho, nodes_vel, q) + neq, nodes_pdf).astype(F32)
     vel = np.where(t == 2, vel_ext, nodes_vel).astype(F32)
-    pdf = np.where(t == 2, calc_eq(rho, vel) + neq, pdf).astype(F32)
+    pdf = np.where(t == 2, calc_eq(rho, vel, q) + neq, pdf).astype(F32)
     return pdf, rho, vel
 
 
@@ -118,7 +145,7 @@ def face_fluxes(geo, cells_pdf, nodes_pdf, dt: F32) -> np.ndarray:
     ghost_r = m + (m - cells_pdf[s0]) * (d1 / d0)
     left = np.where((s0 == -1)[:, None], ghost_l, cells_pdf[s0])
     right = np.where((s1 == -1)[:, None], ghost_r, cells_pdf[s1])
-    v = _fold(KSI_F[None, :, :] * n[:, None, :], 2)            # [F,9]
+    v = _fold(ksi(cells_pdf.shape[1])[None, :, :] * n[:, None, :], 2)  # [F,Q]
     if geo["scheme"] == "upwind":
         phi = np.where(v >= 0, left, right)
     elif geo["scheme"] == "lax_wendroff":
@@ -160,7 +187,7 @@ def step(geo, state, inv_tau: F32, dt: F32, inv_area=None):
     the pre-update pdf, as the reference leaves them."""
     f = state["cells_pdf"]
     rho, vel = calc_macro(f)
-    eq = calc_eq(rho, vel)
+    eq = calc_eq(rho, vel, f.shape[1])
     npdf, nrho, nvel = node_pdfs(geo, f, eq, rho, vel, state["nodes_pdf"],
                                  state["nodes_rho"], state["nodes_vel"])
     fl = face_fluxes(geo, f, npdf, dt)

@@ -65,8 +65,10 @@ def _static(env, out):
 
 
 def run_case(name, raw, flux_method, tau, bc, steps, record, dim_multiplier=1,
-             perturb=None, seed=0, prebuilt=None):
-    from src.dynamics import D2Q9
+             perturb=None, seed=0, prebuilt=None, lattice="D2Q9"):
+    if ONLY and name not in ONLY:
+        return
+    from src import dynamics
     from src.environment import Environment
     from src.mesher import Mesher
 
@@ -80,7 +82,7 @@ def run_case(name, raw, flux_method, tau, bc, steps, record, dim_multiplier=1,
             me.import_meshpy(mesh)
             me.calc_mesh_properties()
         dt = 0.5 * float(np.min(me.face_lengths))
-        d = D2Q9(tau=tau, delta_t=dt)
+        d = getattr(dynamics, lattice)(tau=tau, delta_t=dt)
         cells, faces, nodes = me.to_env(d, flux_method=flux_method, dim_multiplier=dim_multiplier)
         nodes = bc(me, nodes)
         out.update(raw_points=raw.points, raw_elements=raw.elements, raw_faces=raw.faces,
@@ -98,6 +100,7 @@ def run_case(name, raw, flux_method, tau, bc, steps, record, dim_multiplier=1,
     out["delta_t"] = np.float64(dt)
     out["flux_method"] = np.array(flux_method)
     out["dim_multiplier"] = np.float64(dim_multiplier)
+    out["lattice"] = np.int32(d.NUM_QUIVERS)
     out["steps"] = np.array(sorted(record), dtype=np.int32)
     for s in range(1, steps + 1):
         env = env.step()
@@ -283,7 +286,19 @@ def main(ref_path):
              prebuilt=mixed_quadtri, perturb=perturb_pdf(0.03), seed=3)
     c41 = mg.cavity(n=41, seed=0)
     run_case("cavity41_upwind", c41, "upwind", 0.6, cavity_bc(), 3, {1, 3})
+    # D2Q13 (src/dynamics.py:77-102): 13 velocities, third-order equilibrium
+    run_case("cavity7_d2q13_upwind", c7, "upwind", 0.6, cavity_bc(), 40, {1, 40}, lattice="D2Q13")
+    run_case("channel_d2q13_lw", ch, "lax_wendroff", 0.55, channel_bc(0.41), 30, {1, 30},
+             perturb=perturb_pdf(0.02), seed=5, lattice="D2Q13")
 
+
+ONLY = set()
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # make_golden.py [reference path] [--only name,name]: regenerate some cases
+    args = sys.argv[1:]
+    if "--only" in args:
+        i = args.index("--only")
+        ONLY.update(args[i + 1].split(","))
+        del args[i:i + 2]
+    main(args[0] if args else "/root/reference")

@@ -63,6 +63,11 @@ def expected(g, step):
             "nodes_pdf": g[p + "n_pdf"], "nodes_rho": g[p + "n_rho"], "nodes_vel": g[p + "n_vel"]}
 
 
+def lattice(g) -> int:
+    """Velocities of a golden case's lattice (9 when not recorded)."""
+    return int(g["lattice"]) if "lattice" in g else 9
+
+
 def inv_tau_dt(g):
     tau = float(g["tau"])
     dt = float(g["delta_t"])
@@ -73,10 +78,11 @@ def containers(g):
     """Host containers (this package's) holding a golden case's reference
     containers and initial state."""
     from fvdbm_jax_gb300.containers import Cells, Faces, Nodes
-    from fvdbm_jax_gb300.dynamics import D2Q9
+    from fvdbm_jax_gb300.dynamics import D2Q9, D2Q13
 
     scheme, variant = SCHEMES[str(g["flux_method"])]
-    dyn = D2Q9(float(g["tau"]), float(g["delta_t"]))
+    lat = D2Q13 if lattice(g) == 13 else D2Q9
+    dyn = lat(float(g["tau"]), float(g["delta_t"]))
     N, F, P = g["s0_c_pdf"].shape[0], g["s0_f_pdf"].shape[0], g["s0_n_pdf"].shape[0]
     c = Cells(N, dyn)
     c.face_indices = g["c_face_indices"].astype(np.int32)

@@ -9,12 +9,13 @@ import goldens as G
 pytestmark = pytest.mark.gpu
 
 NOT_FUSABLE = {"mixed_quadtri_upwind", "cavity7_cc_alt_upwind"}
+D2Q13 = {"cavity7_d2q13_upwind", "channel_d2q13_lw"}  # staged kernels only
 
 
 def _cases():
     out = []
     for name in G.names():
-        kernels = ["staged", "auto"] if name in NOT_FUSABLE else ["one", "tile", "tile_split", "fused", "fused_nodes",
+        kernels = ["staged", "auto"] if name in NOT_FUSABLE | D2Q13 else ["one", "tile", "tile_split", "fused", "fused_nodes",
                                                                   "staged"]
         for k in kernels:
             for order in ("none", "rcm", "morton"):
@@ -51,3 +52,22 @@ def test_gpu_matches_reference(name, kernel, order):
         for k, v in ex.items():
             assert np.array_equal(got[k].reshape(v.shape), v, equal_nan=True), (name, kernel, order, s, k)
     env.close()
+
+
+def test_d2q13_rejected_by_d2q9_only_parts():
+    """The fused families, the batch, the monitor and the warm-start
+    initialisation are D2Q9 only and say so."""
+    from fvdbm_jax_gb300 import Batch, Environment
+    g = G.load("cavity7_d2q13_upwind")
+    c, f, n = G.containers(g)
+    with pytest.raises(ValueError, match="D2Q13"):
+        Environment(c, f, n, kernel="fused").init()
+    env = Environment(c, f, n)
+    env.init()
+    assert env.info()["kernel"] == 1
+    from fvdbm_jax_gb300 import _native as nat
+    with pytest.raises(nat.FvdbmError, match="D2Q9"):
+        env.residual()
+    env.close()
+    with pytest.raises(ValueError, match="D2Q13"):
+        Batch([(c, f, n)]).init()
