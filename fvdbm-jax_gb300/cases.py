@@ -76,16 +76,32 @@ def _make(spec):
                          flux=spec["flux"], seed=spec["seed"])
 
 
+def partition_cases(costs, n_parts: int):
+    """Greedy longest-processing-time split of independent cases over
+    n_parts ranks: cases in decreasing cost, each to the currently lightest
+    rank.  Returns one ascending list of case indices per rank."""
+    costs = np.asarray(costs, np.float64)
+    load = np.zeros(n_parts)
+    parts = [[] for _ in range(n_parts)]
+    for i in np.argsort(-costs, kind="stable"):
+        r = int(np.argmin(load))
+        parts[r].append(int(i))
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
 def batch_suite(seed: int = 0, n_cavity: int = 128, n_porous: int = 128, flux: str = "upwind",
                 cavity_cells=(2_000, 60_000), porous_cells=(10_000, 120_000), obstacles=(20, 200),
-                re=(50.0, 400.0), porosity: float = 0.8, workers: int = 0):
+                re=(50.0, 400.0), porosity: float = 0.8, workers: int = 0, rank: int = 0, n_ranks: int = 1):
     """Independent cases of uneven size and Reynolds number: cavities with
     N uniform in ``cavity_cells`` (grid n from N = 2(n-1)^2) and porous squares
     with N uniform in ``porous_cells`` and an obstacle count uniform in
     ``obstacles``; Re uniform in ``re`` sets tau (``tau_from_re``).  Returns a
     list of (dynamics, cells, faces, nodes) and one description per case.
     ``workers`` > 0 meshes the cases in that many spawned processes (call it
-    before any GPU work of the calling process)."""
+    before any GPU work of the calling process).  With n_ranks > 1 only this
+    rank's share (``partition_cases`` over the target cell counts) is meshed
+    and returned."""
     rng = np.random.default_rng(seed)
     specs = []
     for i in range(n_cavity):
@@ -99,6 +115,9 @@ def batch_suite(seed: int = 0, n_cavity: int = 128, n_porous: int = 128, flux: s
         r = float(rng.uniform(*re))
         specs.append({"kind": "porous", "obstacles": k, "n_target": N, "re": r, "tau": tau_from_re(r),
                       "porosity": porosity, "flux": flux, "seed": seed * 100_003 + n_cavity + i})
+    if n_ranks > 1:
+        target = [2.0 * (s["grid"] - 1) ** 2 if s["kind"] == "cavity" else s["n_target"] for s in specs]
+        specs = [specs[i] for i in partition_cases(target, n_ranks)[rank]]
     if workers > 0:
         import concurrent.futures as cf
         import multiprocessing as mp

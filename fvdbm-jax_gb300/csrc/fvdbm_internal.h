@@ -306,6 +306,9 @@ cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* ce
                                  cudaStream_t s, int q = Q);
 cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
                                 cudaStream_t s, int q = Q);
+// D2Q9 rho [N] and vel [N][2] of a pdf buffer in reference order
+cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_new, float* rho, float* vel,
+                              cudaStream_t s);
 // D2Q13 (d2q13.cu): the staged step, the face fluxes alone, read-back macros
 cudaError_t launch13_step(const DevPlan& p, const float* fin, float* flux, float* fout, cudaStream_t s);
 cudaError_t launch13_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);

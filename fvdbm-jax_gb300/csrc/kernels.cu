@@ -672,6 +672,29 @@ __global__ void __launch_bounds__(256) k_macros(DevPlan p, const float* __restri
   for (int q = 0; q < Q; ++q) o[q * 32] = eq[q];
 }
 
+// rho [N] and vel [N][2] of a pdf buffer, written directly in reference
+// order (cell_new: reference -> device).
+__global__ void __launch_bounds__(256) k_macros_ref(DevPlan p, const float* __restrict__ f,
+                                                    const int* __restrict__ cell_new, float* __restrict__ rho_o,
+                                                    float* __restrict__ vel_o) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= p.N) return;
+  float fc[Q];
+  load_cell(f, cell_new[c], fc);
+  float rho, ux, uy;
+  macros(fc, rho, ux, uy);
+  rho_o[c] = rho;
+  vel_o[2 * size_t(c)] = ux;
+  vel_o[2 * size_t(c) + 1] = uy;
+}
+
+cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_new, float* rho, float* vel,
+                              cudaStream_t s) {
+  if (p.N == 0) return cudaSuccess;
+  k_macros_ref<<<(p.N + 255) / 256, 256, 0, s>>>(p, f, cell_new, rho, vel);
+  return cudaGetLastError();
+}
+
 // [N][9] reference order -> AoSoA device order.
 template <int QQ>
 __global__ void k_aos_to_cells(const float* __restrict__ src, float* __restrict__ dst,

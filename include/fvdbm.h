@@ -58,7 +58,8 @@ extern "C" {
 #define FVDBM_ORDER_MORTON 2 /* Z-order of cell_xy (needs cell_xy) */
 
 /* Kernel family for the step. */
-#define FVDBM_KERNEL_AUTO 0       /* fastest family the mesh allows */
+#define FVDBM_KERNEL_AUTO 0       /* fastest family the mesh allows (FUSED_NODES from 2^18 cells,
+                                     FUSED below, STAGED when the fused kernels cannot run) */
 #define FVDBM_KERNEL_STAGED 1     /* node BC + face flux + cell gather (3 kernels) */
 #define FVDBM_KERNEL_FUSED 2      /* node BC + fused cell kernel (2 kernels) */
 #define FVDBM_KERNEL_TILE 3       /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
