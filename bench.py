@@ -575,6 +575,19 @@ def run_warmstart(args):
         vel.append(v)
     infer_s = time.perf_counter() - t
     (sw, stw, restarted), warm_s, fin_w = timed((np.concatenate(rho), np.concatenate(vel)))
+    # the plain solver as a user runs it: each case alone from the uniform start
+    from fvdbm_jax_gb300 import Environment
+    seq_s, seq_steps = 0.0, 0
+    for case in evalc:
+        env = Environment(*case[1:4])
+        env.init()
+        env.sync()
+        t1 = time.perf_counter()
+        n_s, _ = env.run_to_steady(thr, every, cap)
+        env.sync()
+        seq_s += time.perf_counter() - t1
+        seq_steps += n_s
+        env.close()
     # accuracy of the prediction against the plain run's steady state
     rho_p, vel_p = WS.macros(fin_p["pdf"])
     pr, pv = np.concatenate(rho), np.concatenate(vel)
@@ -582,6 +595,8 @@ def run_warmstart(args):
     line = {"metric": f"time-to-steady @{thr:g} resid, warm vs plain (held-out porous squares)",
             "value": round(warm_s, 3), "unit": "s", "higher_is_better": False,
             "plain_s": round(plain_s, 3), "speedup_time": round(plain_s / warm_s, 2),
+            "plain_one_at_a_time_s": round(seq_s, 3), "plain_one_at_a_time_steps": int(seq_steps),
+            "speedup_batched_warm_vs_plain_one_at_a_time": round(seq_s / warm_s, 2),
             "steps_plain": int(sp_.sum()), "steps_warm": int(sw.sum()),
             "speedup_steps": round(float(sp_.sum()) / max(float(sw.sum()), 1.0), 2),
             "converged_plain": int(np.sum(stp == 1)), "converged_warm": int(np.sum(stw == 1)),
