@@ -23,6 +23,21 @@ static __constant__ float c_W[Q] = {(float)(4.0 / 9.0),  (float)(1.0 / 9.0),  (f
 
 __device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
 
+// Paired float32 arithmetic (sm_100+ f32x2 instructions): each lane is the
+// IEEE round-to-nearest operation of the scalar form, so paired and scalar
+// evaluation give identical bits; the pairs halve the issued instructions.
+// One rule keeps it so: a paired product never feeds a paired sum.  The
+// compiler contracts that pair into a fused multiply-add (one rounding)
+// despite --fmad=false and the _rn forms; a scalar sum of a paired product,
+// and paired sums of scalar results, stay separately rounded.
+#ifndef FVDBM_PAIRED
+#define FVDBM_PAIRED 1
+#endif
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// a - b == a + (-b) exactly (signed zeros included)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+
 // Programmatic dependent launch: wait until the previous kernel in the
 // stream has completed and its writes are visible (a no-op when the kernel
 // was launched without the attribute); let the next kernel start launching.
@@ -135,8 +150,19 @@ __device__ __forceinline__ void macros(const float f[Q], float& rho, float& ux, 
   r = r + f[8];
   float mx, my;
   if (finite(r)) {
+#if FVDBM_PAIRED
+    // (mx, my) folded side by side
+    float2 m = sub2(make_float2(f[1], f[2]), make_float2(f[3], f[4]));
+    m = add2(m, make_float2(f[5], f[5]));
+    m = add2(m, make_float2(-f[6], f[6]));
+    m = sub2(m, make_float2(f[7], f[7]));
+    m = add2(m, make_float2(f[8], -f[8]));
+    mx = m.x;
+    my = m.y;
+#else
     mx = ((((f[1] - f[3]) + f[5]) - f[6]) - f[7]) + f[8];
     my = ((((f[2] - f[4]) + f[5]) + f[6]) - f[7]) - f[8];
+#endif
   } else {
     macros_literal(f, mx, my);
   }
@@ -187,6 +213,26 @@ __device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPla
     x6 = cdiv(a6, p.d_c2);
     y6 = cdiv(a6 * a6, p.d_c4x2);
   }
+#if FVDBM_PAIRED
+  // (s_1, s_3), (s_2, s_4), (s_5, s_7), (s_6, s_8) share x, y: one pair each
+  const float2 one = make_float2(1.0f, 1.0f), tt = make_float2(t, t);
+  const float2 s13 = sub2(add2(add2(one, make_float2(x1, -x1)), make_float2(y1, y1)), tt);
+  const float2 s24 = sub2(add2(add2(one, make_float2(x2, -x2)), make_float2(y2, y2)), tt);
+  const float2 s57 = sub2(add2(add2(one, make_float2(x5, -x5)), make_float2(y5, y5)), tt);
+  const float2 s68 = sub2(add2(add2(one, make_float2(x6, -x6)), make_float2(y6, y6)), tt);
+  const float w0 = c_W[0] * rho, w1 = c_W[1] * rho, w5 = c_W[5] * rho;
+  const float2 w11 = make_float2(w1, w1), w55 = make_float2(w5, w5);
+  const float2 o13 = mul2(w11, s13), o24 = mul2(w11, s24), o57 = mul2(w55, s57), o68 = mul2(w55, s68);
+  out[0] = w0 * (1.0f - t);
+  out[1] = o13.x;
+  out[3] = o13.y;
+  out[2] = o24.x;
+  out[4] = o24.y;
+  out[5] = o57.x;
+  out[7] = o57.y;
+  out[6] = o68.x;
+  out[8] = o68.y;
+#else
   float s[Q];
   s[0] = 1.0f - t;
   s[1] = ((1.0f + x1) + y1) - t;
@@ -199,6 +245,7 @@ __device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPla
   s[8] = ((1.0f - x6) + y6) - t;
 #pragma unroll
   for (int q = 0; q < Q; ++q) out[q] = (c_W[q] * rho) * s[q];
+#endif
 }
 
 // One component q of feq9, bitwise equal to feq9(...)[q].

@@ -275,6 +275,26 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
     lw_interp(v, __uint_as_float(__ldg(hb + HR.r(k) * 32)), __uint_as_float(__ldg(hb + HR.d2(k) * 32)),
               dt, p.finite_n != 0, w);
   const float scale = (VARIANT == 1) ? __uint_as_float(__ldg(hb + HR.sc(k) * 32)) : 1.0f;
+#if FVDBM_PAIRED
+  if (SCHEME == 0 && VARIANT == 0) {
+    // paired products, scalar sums (a paired sum of paired products would be
+    // contracted into a fused multiply-add)
+    float phi[Q], x[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) phi[q] = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
+    const float2 L2 = make_float2(Ls, Ls);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float2 x2 = mul2(mul2(make_float2(phi[2 * j], phi[2 * j + 1]), make_float2(v[2 * j], v[2 * j + 1])), L2);
+      x[2 * j] = x2.x;
+      x[2 * j + 1] = x2.y;
+    }
+    x[8] = (phi[8] * v[8]) * Ls;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) acc[q] = FIRST ? x[q] : acc[q] + x[q];
+    return;
+  }
+#endif
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     float phi;
