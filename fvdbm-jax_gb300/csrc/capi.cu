@@ -75,9 +75,13 @@ constexpr int kResidualChunk = 1024;  // cells per partial sum of the monitor
 // whose exhaustive check on this device found no dividend that it rounds
 // differently from IEEE division; results are cached per device and divisor.
 std::mutex g_cdiv_mu;
-std::map<std::pair<int, uint32_t>, bool> g_cdiv_ok;
+std::map<std::pair<int, uint32_t>, std::pair<bool, bool>> g_cdiv_ok;  // (five-op ok, two-op ok)
 
-cudaError_t run_cdiv_check(float y, float zr, cudaStream_t s, unsigned long long* bad,
+// zl = RN(1/y - RN(1/y)): 1/y in double carries 53 bits, the difference is
+// exact in double, and its float rounding is the low word.
+float cdiv_low(float y, float zr) { return float(1.0 / double(y) - double(zr)); }
+
+cudaError_t run_cdiv_check(float y, float zr, float zl, int two, cudaStream_t s, unsigned long long* bad,
                            unsigned* example) {
   unsigned long long* d_bad = nullptr;
   unsigned* d_ex = nullptr;
@@ -86,7 +90,7 @@ cudaError_t run_cdiv_check(float y, float zr, cudaStream_t s, unsigned long long
   e = cudaMalloc(&d_ex, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ex, 0xFF, sizeof(unsigned), s);
-  if (e == cudaSuccess) e = launch_cdiv_check(y, zr, d_bad, d_ex, s);
+  if (e == cudaSuccess) e = launch_cdiv_check(y, zr, zl, two, d_bad, d_ex, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(example, d_ex, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -99,30 +103,32 @@ cudaError_t make_cdiv(int device, float y, cudaStream_t s, CDiv* out) {
   const float zr = 1.0f / y;
   out->y = y;
   out->zr = zr;
+  out->zl = 0.0f;
   out->ok = 0;
+  out->two = 0;
   uint32_t bits;
   std::memcpy(&bits, &y, 4);
   const auto key = std::make_pair(device, bits);
+  if (!(std::fabs(y) > 0.0f) || !std::isfinite(y) || !std::isfinite(zr)) return cudaSuccess;
+  out->zl = cdiv_low(y, zr);
   {
     std::lock_guard<std::mutex> lk(g_cdiv_mu);
     auto it = g_cdiv_ok.find(key);
     if (it != g_cdiv_ok.end()) {
-      out->ok = it->second ? 1 : 0;
+      out->ok = it->second.first ? 1 : 0;
+      out->two = it->second.second ? 1 : 0;
       return cudaSuccess;
     }
   }
-  if (!(std::fabs(y) > 0.0f) || !std::isfinite(y) || !std::isfinite(zr)) {
-    std::lock_guard<std::mutex> lk(g_cdiv_mu);
-    g_cdiv_ok[key] = false;
-    return cudaSuccess;
-  }
-  unsigned long long bad = ~0ull;
+  unsigned long long bad = ~0ull, bad2 = ~0ull;
   unsigned example = 0;
-  cudaError_t e = run_cdiv_check(y, zr, s, &bad, &example);
+  cudaError_t e = run_cdiv_check(y, zr, out->zl, 0, s, &bad, &example);
+  if (e == cudaSuccess && bad == 0 && std::isfinite(out->zl)) e = run_cdiv_check(y, zr, out->zl, 1, s, &bad2, &example);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lk(g_cdiv_mu);
-  g_cdiv_ok[key] = (bad == 0);
+  g_cdiv_ok[key] = std::make_pair(bad == 0, bad == 0 && bad2 == 0);
   out->ok = (bad == 0) ? 1 : 0;
+  out->two = (bad == 0 && bad2 == 0) ? 1 : 0;
   return cudaSuccess;
 }
 
@@ -464,6 +470,7 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     CR(make_cdiv(h->device, p.c4x2, h->stream, &p.d_c4x2));
     CR(make_cdiv(h->device, p.c2x2, h->stream, &p.d_c2x2));
   }
+  p.cdiv_mode = (p.d_c2.ok && p.d_c4x2.ok && p.d_c2x2.ok) ? ((p.d_c2.two && p.d_c4x2.two && p.d_c2x2.two) ? 2 : 1) : 0;
 
 #define UP(field, vec)                                                        \
   do {                                                                        \
@@ -863,13 +870,18 @@ int fvdbm_step(void* handle, int32_t n_steps) {
 
 int fvdbm_const_div_check(int32_t device, float divisor, uint64_t* mismatches,
                           uint32_t* first_mismatch) {
-  if (!mismatches || !first_mismatch) return FVDBM_EINVAL;
+  return fvdbm_const_div_check_form(device, divisor, 5, mismatches, first_mismatch);
+}
+
+int fvdbm_const_div_check_form(int32_t device, float divisor, int32_t form, uint64_t* mismatches,
+                               uint32_t* first_mismatch) {
+  if (!mismatches || !first_mismatch || (form != 5 && form != 2)) return FVDBM_EINVAL;
   cudaError_t e = cudaSetDevice(device);
   cudaStream_t s = nullptr;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   unsigned long long bad = 0;
   unsigned ex = 0xFFFFFFFFu;
-  if (e == cudaSuccess) e = run_cdiv_check(divisor, 1.0f / divisor, s, &bad, &ex);
+  if (e == cudaSuccess) e = run_cdiv_check(divisor, 1.0f / divisor, cdiv_low(divisor, 1.0f / divisor), form == 2, s, &bad, &ex);
   if (s) cudaStreamDestroy(s);
   if (e != cudaSuccess) {
     std::lock_guard<std::mutex> lk(g_err_mu);
@@ -1126,7 +1138,7 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->launches_per_step = node_launch + (h->one || h->tile || h->batch ? 1 : (h->fused ? 1 : 2));
   info->padded_cells = hp.Np;
   info->ctas_per_sm = h->tile ? tile_ctas_per_sm(h->dp) : 0;
-  info->const_division = (h->dp.d_c2.ok && h->dp.d_c4x2.ok && h->dp.d_c2x2.ok) ? 1 : 0;
+  info->const_division = h->dp.cdiv_mode;
   info->bytes_per_step = hp.bytes_per_step;
   info->device_bytes = h->device_bytes;
   return FVDBM_OK;

@@ -155,12 +155,14 @@ struct UnionMesh {
 };
 std::string build_union(const fvdbm_mesh_t* meshes, int S, UnionMesh& u);
 
-// Division by a divisor known in advance: y and zr = RN(1/y).  ok says the
-// three-operation form was verified against IEEE division for every float32
-// dividend on this device (else the kernels divide with '/').
+// Division by a divisor known in advance: y, zr = RN(1/y) and
+// zl = RN(1/y - zr).  ok says the correction form (five operations) was
+// verified against IEEE division for every float32 dividend on this device
+// (else the kernels divide with '/'); two says the same of the two-operation
+// form, which is then used instead.
 struct CDiv {
-  float y, zr;
-  int ok;
+  float y, zr, zl;
+  int ok, two;
 };
 
 struct DevPlan {
@@ -172,6 +174,7 @@ struct DevPlan {
   float c6x2;  // D2Q13: 2 C^6
   int q;       // lattice velocities: 9 or 13
   CDiv d_c2, d_c4x2, d_c2x2;
+  int cdiv_mode;  // 2: all three two-operation forms verified, 1: five-operation, 0: neither
   // staged faces
   const int* fs0;
   const int* fs1;
@@ -299,7 +302,7 @@ cudaError_t launch_copy_cells(const float* src, float* dst, int c0, int c1, cuda
 // Counts the float32 dividends x (all 2^32 bit patterns) for which the
 // known-divisor division differs from x / y, and the lowest such bit pattern;
 // *bad must be zeroed and *example set to 0xFFFFFFFF.
-cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsigned* example,
+cudaError_t launch_cdiv_check(float y, float zr, float zl, int two, unsigned long long* bad, unsigned* example,
                               cudaStream_t s);
 // [N][q] reference order <-> AoSoA device order (cell_new: reference -> device)
 cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* cell_new, int N,

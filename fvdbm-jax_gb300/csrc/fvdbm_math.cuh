@@ -74,12 +74,20 @@ __device__ __forceinline__ float cdiv_fast(float x, float y, float zr) {
   return __fmaf_rn(r1, zr, q1);
 }
 
+// Brisebarre, Muller and Raina (same paper, Algorithm 1): with zh = RN(1/y)
+// and zl = RN(1/y - zh), RN(x*zh + RN(x*zl)) equals RN(x/y) for every x for
+// many divisors y (not all); k_cdiv_check decides for the divisor at hand.
+__device__ __forceinline__ float cdiv_two(float x, float zh, float zl) {
+  return __fmaf_rn(x, zh, __fmul_rn(x, zl));
+}
+
 // The remainders are exact only while they stay above the subnormal range,
 // so tiny dividends (|x| < 2^-100) and quotients outside the normal range
-// take x/y; x == 0 gives +-0 either way.
+// take x/y; x == 0 gives +-0 either way.  The same domain serves the
+// two-operation form (x*zl stays normal there).
 __device__ __forceinline__ float cdiv(float x, const CDiv& d) {
   if (d.ok) {
-    const float q = cdiv_fast(x, d.y, d.zr);
+    const float q = d.two ? cdiv_two(x, d.zr, d.zl) : cdiv_fast(x, d.y, d.zr);
     const float a = fabsf(q);
     if ((fabsf(x) >= 0x1p-100f && a >= FLT_MIN && a <= FLT_MAX) || x == 0.0f) return q;
   }
@@ -191,8 +199,18 @@ __device__ __forceinline__ void feq9(float rho, float ux, float uy, const DevPla
   const float uu = ux * ux + uy * uy;
   const float a5 = ux + uy, a6 = uy - ux;
   float t, x1, y1, x2, y2, x5, y5, x6, y6;
-  if (p.d_c2.ok && p.d_c4x2.ok && p.d_c2x2.ok && cdiv_domain(ux) && cdiv_domain(uy) &&
-      cdiv_domain(a5) && cdiv_domain(a6)) {
+  const bool dom = cdiv_domain(ux) && cdiv_domain(uy) && cdiv_domain(a5) && cdiv_domain(a6);
+  if (p.cdiv_mode == 2 && dom) {
+    t = cdiv_two(uu, p.d_c2x2.zr, p.d_c2x2.zl);
+    x1 = cdiv_two(ux, p.d_c2.zr, p.d_c2.zl);
+    y1 = cdiv_two(ux * ux, p.d_c4x2.zr, p.d_c4x2.zl);
+    x2 = cdiv_two(uy, p.d_c2.zr, p.d_c2.zl);
+    y2 = cdiv_two(uy * uy, p.d_c4x2.zr, p.d_c4x2.zl);
+    x5 = cdiv_two(a5, p.d_c2.zr, p.d_c2.zl);
+    y5 = cdiv_two(a5 * a5, p.d_c4x2.zr, p.d_c4x2.zl);
+    x6 = cdiv_two(a6, p.d_c2.zr, p.d_c2.zl);
+    y6 = cdiv_two(a6 * a6, p.d_c4x2.zr, p.d_c4x2.zl);
+  } else if (p.cdiv_mode == 1 && dom) {
     t = cdiv_fast(uu, p.d_c2x2.y, p.d_c2x2.zr);
     x1 = cdiv_fast(ux, p.d_c2.y, p.d_c2.zr);
     y1 = cdiv_fast(ux * ux, p.d_c4x2.y, p.d_c4x2.zr);

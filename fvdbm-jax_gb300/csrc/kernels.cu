@@ -245,17 +245,14 @@ __global__ void __launch_bounds__(256) k_stencil_macros(DevPlan p, const float* 
 // (recomputed from the canonical slot-0/slot-1 pair, so both neighbours get
 // bit-identical fluxes without a flux array or atomics), the signed flux sum
 // and the BGK/explicit-Euler update (src/containers.py:107-121).
-template <int SCHEME, int VARIANT, bool FIRST, bool GHOST_CG>
-__device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin,
-                                           const unsigned* __restrict__ hb, int k, int code, float nx,
-                                           float ny, float Ls, float dt, const float f[Q], float acc[Q]) {
-  const HfRows HR{3, SCHEME, VARIANT};
+// The pdfs across face slot `code`: the neighbour cell's, or the ghost value
+// m + (m - f_known)*(d_ghost/d_known), m = mean of the face's two end-node
+// pdfs (src/containers.py:280-287, utils/utils.py:153).
+template <bool GHOST_CG>
+__device__ __forceinline__ void face_other(const DevPlan& p, const float* __restrict__ fin, int code,
+                                           const float f[Q], float o[Q]) {
   const int other = code >> HF_SHIFT;
-  const bool slot1 = (code & HF_SLOT1) != 0;
-  float o[Q];
   if (code & HF_GHOST) {
-    // ghost = m + (m - f_known)*(d_ghost/d_known), m = mean of the face's two
-    // end-node pdfs (src/containers.py:280-287, utils/utils.py:153)
     const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
     const float rg = __ldg(p.gh_r + other);
 #pragma unroll
@@ -268,6 +265,16 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
   } else {
     load_cell(fin, other, o);
   }
+}
+
+// Flux of face slot k from this cell's pdfs f and the pdfs o across it,
+// signed for this cell, into acc (first slot: assigned).
+template <int SCHEME, int VARIANT, bool FIRST>
+__device__ __forceinline__ void face_flux(const DevPlan& p, const unsigned* __restrict__ hb, int k, int code,
+                                          float nx, float ny, float Ls, float dt, const float f[Q],
+                                          const float o[Q], float acc[Q]) {
+  const HfRows HR{3, SCHEME, VARIANT};
+  const bool slot1 = (code & HF_SLOT1) != 0;
   float v[Q];
   xi_dot_n(nx, ny, p.finite_n != 0, v);
   float w[Q];
@@ -309,6 +316,15 @@ __device__ __forceinline__ void fused_face(const DevPlan& p, const float* __rest
     if (VARIANT == 1) x = x * scale;
     acc[q] = FIRST ? x : acc[q] + x;
   }
+}
+
+template <int SCHEME, int VARIANT, bool FIRST, bool GHOST_CG>
+__device__ __forceinline__ void fused_face(const DevPlan& p, const float* __restrict__ fin,
+                                           const unsigned* __restrict__ hb, int k, int code, float nx,
+                                           float ny, float Ls, float dt, const float f[Q], float acc[Q]) {
+  float o[Q];
+  face_other<GHOST_CG>(p, fin, code, f, o);
+  face_flux<SCHEME, VARIANT, FIRST>(p, hb, k, code, nx, ny, Ls, dt, f, o, acc);
 }
 
 __device__ __forceinline__ void prefetch_l2(const void* ptr, uint32_t bytes) {
@@ -746,12 +762,13 @@ __global__ void k_soa_to_aos(const float* __restrict__ src, float* __restrict__ 
   for (int q = 0; q < rows; ++q) dst[size_t(c) * rows + q] = src[size_t(q) * Np + d];
 }
 
-// Exhaustive check of cdiv against IEEE division: every float32 bit pattern
-// as dividend; counts the dividends whose quotients differ in value (NaN
-// matches NaN).  Not on the step path; runs once per divisor per process.
-__global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, unsigned long long* bad,
+// Exhaustive check of cdiv (five-operation form, or the two-operation form
+// when two is set) against IEEE division: every float32 bit pattern as
+// dividend; counts the dividends whose quotients differ in value (NaN matches
+// NaN).  Not on the step path; runs once per divisor and form per process.
+__global__ void __launch_bounds__(256) k_cdiv_check(float y, float zr, float zl, int two, unsigned long long* bad,
                                                     unsigned* example) {
-  const CDiv d{y, zr, 1};
+  const CDiv d{y, zr, zl, 1, two};
   unsigned long long local = 0;
   unsigned ex = 0xFFFFFFFFu;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -978,12 +995,12 @@ cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* v
   return cudaGetLastError();
 }
 
-cudaError_t launch_cdiv_check(float y, float zr, unsigned long long* bad, unsigned* example,
+cudaError_t launch_cdiv_check(float y, float zr, float zl, int two, unsigned long long* bad, unsigned* example,
                               cudaStream_t s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_cdiv_check<<<sms * 8, 256, 0, s>>>(y, zr, bad, example);
+  k_cdiv_check<<<sms * 8, 256, 0, s>>>(y, zr, zl, two, bad, example);
   return cudaGetLastError();
 }
 

@@ -123,9 +123,11 @@ typedef struct fvdbm_info {
   int32_t launches_per_step;
   int32_t padded_cells;     /* row stride of the [9][Np] pdf */
   int32_t ctas_per_sm;      /* resident CTAs per SM of the tile kernel (0 if unused) */
-  int32_t const_division;   /* 1: divisions by the lattice constants use the
-                               known-divisor form, verified on this device to
-                               equal IEEE division for every float32 dividend */
+  int32_t const_division;   /* divisions by the lattice constants use a
+                               known-divisor form verified on this device to
+                               equal IEEE division for every float32 dividend:
+                               2 the two-operation form, 1 the five-operation
+                               form, 0 neither (IEEE division) */
   double bytes_per_step;    /* algorithmic bytes of one step */
   double device_bytes;      /* device memory held by the handle */
 } fvdbm_info_t;
@@ -177,6 +179,15 @@ int fvdbm_get_face_fluxes(void *handle, float *flux);
  * No counterpart in the reference (it divides with XLA's division). */
 int fvdbm_const_div_check(int32_t device, float divisor, uint64_t *mismatches,
                           uint32_t *first_mismatch);
+
+/* The same check for one form: form 5 is the five-operation correction form
+ * (what fvdbm_const_div_check checks), form 2 the two-operation form
+ * RN(x*zh + RN(x*zl)) with zh = RN(1/divisor), zl = RN(1/divisor - zh)
+ * (Brisebarre, Muller and Raina, IEEE Trans. Computers 53(8), 2004).  The
+ * kernels use form 2 only for divisors that pass both checks.  No
+ * counterpart in the reference. */
+int fvdbm_const_div_check_form(int32_t device, float divisor, int32_t form, uint64_t *mismatches,
+                               uint32_t *first_mismatch);
 
 /* Block until the handle's stream is idle.  Returns FVDBM_EDEVICE when a
  * kernel reported a failure on the device status word (a bounded wait that

@@ -139,27 +139,30 @@ def test_state_round_trip_and_midrun_write(kernel):
     _compare(env, st)
 
 
+@pytest.mark.parametrize("form", [5, 2])
 @pytest.mark.parametrize("which", ["c2", "c4x2", "c2x2"])
-def test_known_divisor_division_exhaustive(which):
-    """Every float32 dividend: the known-divisor division equals IEEE x/y."""
+def test_known_divisor_division_exhaustive(which, form):
+    """Every float32 dividend: the known-divisor division (five- and
+    two-operation forms) equals IEEE x/y."""
     import ctypes as C
     from fvdbm_jax_gb300 import D2Q9
     from fvdbm_jax_gb300 import _native as nat
     y = float(getattr(D2Q9(0.6, 0.1), which))
     bad, ex = C.c_uint64(), C.c_uint32()
-    nat.check(nat.lib().fvdbm_const_div_check(0, y, C.byref(bad), C.byref(ex)))
+    nat.check(nat.lib().fvdbm_const_div_check_form(0, y, form, C.byref(bad), C.byref(ex)))
     x = np.array([ex.value], np.uint32).view(np.float32)[0]
     assert bad.value == 0, f"{bad.value} mismatches, first dividend {x!r} (bits {ex.value:#x})"
 
 
 def test_known_divisor_division_verified_and_used():
-    """The three lattice-constant divisors pass the exhaustive check (every
-    float32 dividend gives the IEEE quotient), so the kernels use it."""
+    """The three lattice-constant divisors pass the exhaustive check of the
+    two-operation form (every float32 dividend gives the IEEE quotient), so
+    the kernels use that form."""
     from fvdbm_jax_gb300 import Environment, meshgen
     m, dyn, c, f, n = _case(meshgen.cavity(n=5))
     env = Environment(c, f, n)
     env.init()
-    assert env.info()["const_division"] == 1
+    assert env.info()["const_division"] == 2
 
 
 @pytest.mark.parametrize("kernel", ["auto", "fused"])
