@@ -463,6 +463,8 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   p.c4x2 = params->c4x2;
   p.c2x2 = params->c2x2;
   p.c6x2 = params->c6x2;
+  p.one = 1.0f;
+  p.neg_one = -1.0f;
   p.q = hp.q;
   p.finite_n = hp.finite_n ? 1 : 0;
   if (hp.q == 9) {  // (the D2Q13 kernels divide with '/')

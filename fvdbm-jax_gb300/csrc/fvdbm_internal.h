@@ -171,6 +171,7 @@ struct DevPlan {
   int last_cell;
   int finite_n;  // every face normal is finite (enables the symmetric xi.n form)
   float inv_tau, dt, c2, c4x2, c2x2;
+  float one, neg_one;  // 1 and -1 as run-time values (paired sums of paired products)
   float c6x2;  // D2Q13: 2 C^6
   int q;       // lattice velocities: 9 or 13
   CDiv d_c2, d_c4x2, d_c2x2;

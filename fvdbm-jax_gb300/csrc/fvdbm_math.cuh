@@ -26,10 +26,13 @@ __device__ __forceinline__ bool finite(float x) { return fabsf(x) <= FLT_MAX; }
 // Paired float32 arithmetic (sm_100+ f32x2 instructions): each lane is the
 // IEEE round-to-nearest operation of the scalar form, so paired and scalar
 // evaluation give identical bits; the pairs halve the issued instructions.
-// One rule keeps it so: a paired product never feeds a paired sum.  The
+// One rule keeps it so: a paired product never feeds a paired add.  The
 // compiler contracts that pair into a fused multiply-add (one rounding)
-// despite --fmad=false and the _rn forms; a scalar sum of a paired product,
-// and paired sums of scalar results, stay separately rounded.
+// despite --fmad=false and the _rn forms (and rewrites a*1 + x with a
+// literal 1 into an add first).  A sum that takes a paired product is
+// written as the multiply-add a*one + x with one = 1 held in a run-time
+// value: a*one is exact, so it rounds as a + x does, signed zeros included,
+// and a multiply-add has no product left to contract.
 #ifndef FVDBM_PAIRED
 #define FVDBM_PAIRED 1
 #endif
@@ -37,6 +40,9 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 // a - b == a + (-b) exactly (signed zeros included)
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+// a*s + x for s = (1, 1) or (-1, -1) given at run time: x + a or x - a,
+// where x may be a paired product
+__device__ __forceinline__ float2 fold2(float2 a, float2 s, float2 x) { return __ffma2_rn(a, s, x); }
 
 // Programmatic dependent launch: wait until the previous kernel in the
 // stream has completed and its writes are visible (a no-op when the kernel

@@ -284,21 +284,19 @@ __device__ __forceinline__ void face_flux(const DevPlan& p, const unsigned* __re
   const float scale = (VARIANT == 1) ? __uint_as_float(__ldg(hb + HR.sc(k) * 32)) : 1.0f;
 #if FVDBM_PAIRED
   if (SCHEME == 0 && VARIANT == 0) {
-    // paired products, scalar sums (a paired sum of paired products would be
-    // contracted into a fused multiply-add)
-    float phi[Q], x[Q];
+    float phi[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) phi[q] = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
-    const float2 L2 = make_float2(Ls, Ls);
+    const float2 L2 = make_float2(Ls, Ls), one2 = make_float2(p.one, p.one);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const float2 x2 = mul2(mul2(make_float2(phi[2 * j], phi[2 * j + 1]), make_float2(v[2 * j], v[2 * j + 1])), L2);
-      x[2 * j] = x2.x;
-      x[2 * j + 1] = x2.y;
+      const float2 x = mul2(mul2(make_float2(phi[2 * j], phi[2 * j + 1]), make_float2(v[2 * j], v[2 * j + 1])), L2);
+      const float2 a = FIRST ? x : fold2(make_float2(acc[2 * j], acc[2 * j + 1]), one2, x);
+      acc[2 * j] = a.x;
+      acc[2 * j + 1] = a.y;
     }
-    x[8] = (phi[8] * v[8]) * Ls;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) acc[q] = FIRST ? x[q] : acc[q] + x[q];
+    const float x8 = (phi[8] * v[8]) * Ls;
+    acc[8] = FIRST ? x8 : acc[8] + x8;
     return;
   }
 #endif
@@ -354,11 +352,29 @@ __device__ __forceinline__ void fused_cell_f(const DevPlan& p, const float* __re
   }
   float* o = fout + cell_base(i, Q);
   float fn[Q];
+#if FVDBM_PAIRED
+  // f + dt*(inv_tau*(eq - f) - acc), pairwise
+  const float2 it2 = make_float2(inv_tau, inv_tau), dt2 = make_float2(dt, dt);
+  const float2 one2 = make_float2(p.one, p.one), m12 = make_float2(p.neg_one, p.neg_one);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float2 f2 = make_float2(f[2 * j], f[2 * j + 1]);
+    const float2 d = fold2(f2, m12, make_float2(eq[2 * j], eq[2 * j + 1]));    // eq - f
+    const float2 u = fold2(make_float2(acc[2 * j], acc[2 * j + 1]), m12, mul2(it2, d));  // - acc
+    const float2 r = fold2(f2, one2, mul2(dt2, u));                               // f + ...
+    fn[2 * j] = r.x;
+    fn[2 * j + 1] = r.y;
+  }
+  fn[8] = f[8] + dt * (inv_tau * (eq[8] - f[8]) - acc[8]);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) o[q * 32] = fn[q];
+#else
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     fn[q] = f[q] + dt * (inv_tau * (eq[q] - f[q]) - acc[q]);
     o[q * 32] = fn[q];
   }
+#endif
   if (RECORD && i >= p.stencil_start && i < p.stencil_end) record_stencil(p, i, fn);
 }
 
