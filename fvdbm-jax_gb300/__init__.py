@@ -10,11 +10,11 @@ the ``Environment.init``/``Environment.step`` path of MADALERAU/FVDBM-JAX.
     env = Environment(cells, faces, nodes); env.init()
     env = env.step()
 """
-from .dynamics import D2Q9
+from .dynamics import D2Q9, D2Q13
 from .containers import Cells, Faces, Nodes
 from .mesher import Mesher
 from .environment import Environment
 from .batch import Batch
 from . import meshgen
 
-__all__ = ["D2Q9", "Cells", "Faces", "Nodes", "Mesher", "Environment", "Batch", "meshgen"]
+__all__ = ["D2Q9", "D2Q13", "Cells", "Faces", "Nodes", "Mesher", "Environment", "Batch", "meshgen"]
