@@ -132,6 +132,17 @@ cudaError_t make_cdiv(int device, float y, cudaStream_t s, CDiv* out) {
   return cudaSuccess;
 }
 
+// Device address of host memory the device reads and writes directly
+// (page-locked memory known to CUDA), or null for any other pointer.
+void* host_mapped(const void* ptr) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
 int fail(Handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
   return code;
@@ -802,9 +813,17 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
   Handle* h = static_cast<Handle*>(handle);
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
+  bool read_later = false;  // a page-locked source is read by the stream after this returns
   if (cell_pdf && hp.N > 0) {
-    CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(hp.q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
-    CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream, hp.q));
+    const float* mapped = static_cast<const float*>(host_mapped(cell_pdf));
+    if (mapped && (reinterpret_cast<uintptr_t>(mapped) & 15) == 0) {
+      // one pass over the host link, scattered on arrival
+      CK(launch_host_to_cells(mapped, h->f[h->cur], h->d_cell_new, hp.N, h->stream, hp.q));
+    } else {
+      CK(cudaMemcpyAsync(h->stage, cell_pdf, size_t(hp.q) * hp.N * 4, cudaMemcpyHostToDevice, h->stream));
+      CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream, hp.q));
+    }
+    read_later = mapped != nullptr;
     if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
     // a retired batch case keeps its state in both buffers
     for (size_t s = 0; s < h->active.size(); ++s)
@@ -820,6 +839,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
     int rc = upload_nodes(h);
     if (rc != FVDBM_OK) return rc;
   }
+  if (read_later) CK(cudaStreamSynchronize(h->stream));  // the caller may reuse its arrays on return
   return FVDBM_OK;
 }
 
@@ -968,8 +988,16 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
     CK(cudaStreamSynchronize(h->stream));
   }
   if ((rho || vel) && !pdf_eq && N > 0 && hp.q == 9 && h->steps_done > 0) {
-    // rho and vel only: one kernel writes both in reference order, two
-    // copies, one synchronisation (the staging buffer holds 9N >= 3N floats)
+    // rho and vel only: one kernel writes both in reference order, straight
+    // into page-locked host arrays when both are, else into the staging
+    // buffer (9N >= 3N floats) with two copies; one synchronisation
+    float* hr = rho ? static_cast<float*>(host_mapped(rho)) : nullptr;
+    float* hv = vel ? static_cast<float*>(host_mapped(vel)) : nullptr;
+    if ((!rho || hr) && (!vel || hv)) {
+      CK(launch_macros_ref(h->dp, h->f[h->cur ^ 1], h->d_cell_new, hr, hv, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      return check_status(h);
+    }
     float* sr = h->stage;
     float* sv = h->stage + N;
     CK(launch_macros_ref(h->dp, h->f[h->cur ^ 1], h->d_cell_new, sr, sv, h->stream));

@@ -310,7 +310,11 @@ cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* ce
                                  cudaStream_t s, int q = Q);
 cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
                                 cudaStream_t s, int q = Q);
-// D2Q9 rho [N] and vel [N][2] of a pdf buffer in reference order
+// the scatter reading page-locked host memory directly (src 16-byte aligned)
+cudaError_t launch_host_to_cells(const float* src_host, float* dst, const int* cell_new, int N,
+                                 cudaStream_t s, int q = Q);
+// D2Q9 rho [N] and vel [N][2] of a pdf buffer in reference order (either
+// may be null; both may be page-locked host memory)
 cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_new, float* rho, float* vel,
                               cudaStream_t s);
 // D2Q13 (d2q13.cu): the staged step, the face fluxes alone, read-back macros

@@ -283,7 +283,7 @@ __device__ __forceinline__ void face_flux(const DevPlan& p, const unsigned* __re
               dt, p.finite_n != 0, w);
   const float scale = (VARIANT == 1) ? __uint_as_float(__ldg(hb + HR.sc(k) * 32)) : 1.0f;
 #if FVDBM_PAIRED
-  if (SCHEME == 0 && VARIANT == 0) {
+  if constexpr (SCHEME == 0 && VARIANT == 0) {
     float phi[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) phi[q] = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
@@ -297,22 +297,23 @@ __device__ __forceinline__ void face_flux(const DevPlan& p, const unsigned* __re
     }
     const float x8 = (phi[8] * v[8]) * Ls;
     acc[8] = FIRST ? x8 : acc[8] + x8;
-    return;
-  }
+  } else
 #endif
+  {
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    float phi;
-    if (SCHEME == 0) {
-      // upwind: slot 0 when xi.n >= 0, else slot 1
-      phi = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
-    } else {
-      const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
-      phi = lq + (rq - lq) * w[q];
+    for (int q = 0; q < Q; ++q) {
+      float phi;
+      if (SCHEME == 0) {
+        // upwind: slot 0 when xi.n >= 0, else slot 1
+        phi = ((v[q] >= 0.0f) != slot1) ? f[q] : o[q];
+      } else {
+        const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
+        phi = lq + (rq - lq) * w[q];
+      }
+      float x = (phi * v[q]) * Ls;
+      if (VARIANT == 1) x = x * scale;
+      acc[q] = FIRST ? x : acc[q] + x;
     }
-    float x = (phi * v[q]) * Ls;
-    if (VARIANT == 1) x = x * scale;
-    acc[q] = FIRST ? x : acc[q] + x;
   }
 }
 
@@ -726,25 +727,58 @@ __global__ void __launch_bounds__(256) k_macros(DevPlan p, const float* __restri
 
 // rho [N] and vel [N][2] of a pdf buffer, written directly in reference
 // order (cell_new: reference -> device).
+// rho_o / vel_o may be null, or host memory the device addresses directly
+// (each warp then writes whole contiguous spans); vel2: vel_o is 8-byte
+// aligned and (ux, uy) go out as one 8-byte store.
 __global__ void __launch_bounds__(256) k_macros_ref(DevPlan p, const float* __restrict__ f,
                                                     const int* __restrict__ cell_new, float* __restrict__ rho_o,
-                                                    float* __restrict__ vel_o) {
+                                                    float* __restrict__ vel_o, int vel2) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= p.N) return;
   float fc[Q];
   load_cell(f, cell_new[c], fc);
   float rho, ux, uy;
   macros(fc, rho, ux, uy);
-  rho_o[c] = rho;
-  vel_o[2 * size_t(c)] = ux;
-  vel_o[2 * size_t(c) + 1] = uy;
+  if (rho_o) rho_o[c] = rho;
+  if (vel_o) {
+    if (vel2) {
+      reinterpret_cast<float2*>(vel_o)[c] = make_float2(ux, uy);
+    } else {
+      vel_o[2 * size_t(c)] = ux;
+      vel_o[2 * size_t(c) + 1] = uy;
+    }
+  }
 }
 
 cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_new, float* rho, float* vel,
                               cudaStream_t s) {
   if (p.N == 0) return cudaSuccess;
-  k_macros_ref<<<(p.N + 255) / 256, 256, 0, s>>>(p, f, cell_new, rho, vel);
+  const int vel2 = (reinterpret_cast<uintptr_t>(vel) & 7) == 0 ? 1 : 0;
+  k_macros_ref<<<(p.N + 255) / 256, 256, 0, s>>>(p, f, cell_new, rho, vel, vel2);
   return cudaGetLastError();
+}
+
+// [N][QQ] reference order read straight from page-locked host memory (the
+// source must be 16-byte aligned): each block copies its 256 cells'
+// contiguous bytes with 16-byte loads into shared memory, so every byte
+// crosses the host link once, then scatters them to the AoSoA layout.
+template <int QQ>
+__global__ void __launch_bounds__(256) k_host_to_cells(const float* __restrict__ src, float* __restrict__ dst,
+                                                       const int* __restrict__ cell_new, int N) {
+  __shared__ float4 sm[(256 * QQ + 3) / 4];
+  float* smf = reinterpret_cast<float*>(sm);
+  const int c0 = blockIdx.x * 256;
+  const int cells = min(256, N - c0);
+  const int nf = cells * QQ, n4 = nf >> 2;
+  const float* s = src + size_t(c0) * QQ;  // 16-byte aligned: c0 * QQ * 4 is a multiple of 1024
+  for (int k = threadIdx.x; k < n4; k += 256) sm[k] = reinterpret_cast<const float4*>(s)[k];
+  for (int k = (n4 << 2) + threadIdx.x; k < nf; k += 256) smf[k] = s[k];
+  __syncthreads();
+  if (int(threadIdx.x) < cells) {
+    float* o = dst + cell_base(cell_new[c0 + threadIdx.x], QQ);
+#pragma unroll
+    for (int q = 0; q < QQ; ++q) o[q * 32] = smf[threadIdx.x * QQ + q];
+  }
 }
 
 // [N][9] reference order -> AoSoA device order.
@@ -1027,6 +1061,16 @@ cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* ce
     k_aos_to_cells<13><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
   else
     k_aos_to_cells<Q><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_host_to_cells(const float* src_host, float* dst, const int* cell_new, int N,
+                                 cudaStream_t s, int q) {
+  if (N == 0) return cudaSuccess;
+  if (q == 13)
+    k_host_to_cells<13><<<blocks(N, 256), 256, 0, s>>>(src_host, dst, cell_new, N);
+  else
+    k_host_to_cells<Q><<<blocks(N, 256), 256, 0, s>>>(src_host, dst, cell_new, N);
   return cudaGetLastError();
 }
 

@@ -140,7 +140,9 @@ int fvdbm_create(const fvdbm_mesh_t *mesh, const fvdbm_params_t *params, void **
 
 /* The dynamic pytree leaves (Cells.pdf, Nodes.pdf/rho/vel,
  * src/containers.py:33-36,75,321).  NULL leaves are left unchanged.
- * cell_pdf [N][9], node_pdf [P][9], node_rho [P], node_vel [P][2]. */
+ * cell_pdf [N][9], node_pdf [P][9], node_rho [P], node_vel [P][2].  The
+ * arrays are read before the call returns; a page-locked cell_pdf is read
+ * by the device directly over the host link. */
 int fvdbm_set_state(void *handle, const float *cell_pdf, const float *node_pdf,
                     const float *node_rho, const float *node_vel);
 
@@ -162,7 +164,8 @@ int fvdbm_step_phase(void *handle, int32_t phase);
 /* Cells.pdf after the last step, and Cells.rho/vel/pdf_eq as the reference
  * leaves them: the macros of the pdf before the last update
  * (src/environment.py:60-64).  Any pointer may be NULL.  Synchronises.
- * pdf [N][9], rho [N], vel [N][2], pdf_eq [N][9]. */
+ * pdf [N][9], rho [N], vel [N][2], pdf_eq [N][9].  Page-locked rho and vel
+ * arrays are written by the device directly over the host link. */
 int fvdbm_get_cells(void *handle, float *pdf, float *rho, float *vel, float *pdf_eq);
 
 /* Nodes.pdf/rho/vel after the last step.  pdf [P][9], rho [P], vel [P][2]. */
