@@ -66,6 +66,14 @@ struct Handle {
   double* red = nullptr;    // chunk partials, then the 4 totals
   float* d_area = nullptr;  // [Np] cell areas (mass weights) or null
   long long snap_step = -1; // steps_done at the snapshot, -1 = none
+  // read-back beside the step: rho/vel of the last step's input buffer do not
+  // depend on the step, so fvdbm_get_cells computes them on a side stream that
+  // waits only for in_ready, recorded just before a single fvdbm_step(h, 1);
+  // in_ok is cleared by every call that enqueues other work on the state
+  cudaStream_t side = nullptr;  // highest priority: its blocks take SM slots as the step's retire
+  cudaEvent_t in_ready = nullptr;
+  bool in_ok = false;
+  int* status_host = nullptr;  // page-locked copy of *status, filled on the stream before a sync
   std::string err;
 };
 
@@ -282,6 +290,17 @@ int check_status(Handle* h) {
   return FVDBM_OK;
 }
 
+// check_status without a second round trip: the status word is copied on
+// the stream before the synchronisation the caller needs anyway.
+int sync_and_check(Handle* h) {
+  CK(cudaMemcpyAsync(h->status_host, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (*h->status_host != 0)
+    return fail(h, FVDBM_EDEVICE, "device status " + std::to_string(*h->status_host) +
+                                      ": a bounded wait in the tile kernel gave up");
+  return FVDBM_OK;
+}
+
 int get_graph(Handle* h, int parity, cudaGraphExec_t* out) {
   parity += 2 * (h->fnodes ? h->node_cur : 0);
   if (h->graph[parity]) {
@@ -361,6 +380,10 @@ int fvdbm_destroy(void* handle) {
   for (auto& g : h->graph)
     if (g) cudaGraphExecDestroy(g);
   for (void* p : h->allocs) cudaFree(p);
+  if (h->side) cudaStreamSynchronize(h->side);
+  if (h->status_host) cudaFreeHost(h->status_host);
+  if (h->in_ready) cudaEventDestroy(h->in_ready);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return FVDBM_OK;
@@ -405,6 +428,13 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   } while (0)
   CR(cudaSetDevice(h->device));
   CR(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  {
+    int lo = 0, hi = 0;
+    CR(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CR(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi));
+  }
+  CR(cudaHostAlloc(reinterpret_cast<void**>(&h->status_host), sizeof(int), cudaHostAllocDefault));
+  CR(cudaEventCreateWithFlags(&h->in_ready, cudaEventDisableTiming));
   const HostPlan& hp = h->hp;
   DevPlan& p = h->dp;
   h->fused = hp.fusable && params->kernel != FVDBM_KERNEL_STAGED;
@@ -683,6 +713,7 @@ int fvdbm_batch_create(const fvdbm_mesh_t* meshes, const fvdbm_params_t* params,
 int fvdbm_batch_config(void* handle, int32_t block, int32_t prefetch_waves) {
   if (!handle) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
   if ((block != 128 && block != 256) || prefetch_waves < 0 || prefetch_waves > 8)
     return fail(h, FVDBM_EINVAL, "block must be 128 or 256 and prefetch_waves 0..8");
@@ -736,6 +767,7 @@ int fvdbm_batch_residual(void* handle, double* res_u, double* mass) {
 int fvdbm_batch_set_active(void* handle, const int32_t* active) {
   if (!handle || !active) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
@@ -761,6 +793,7 @@ int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_ever
                               int64_t* steps, double* res_u, int32_t* status) {
   if (!handle || !max_steps || !steps || !res_u || !status) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
   if (check_every <= 0) return fail(h, FVDBM_EINVAL, "check_every <= 0");
   const int S = h->hp.S;
@@ -811,6 +844,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
                     const float* node_vel) {
   if (!handle) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
   bool read_later = false;  // a page-locked source is read by the stream after this returns
@@ -846,6 +880,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
 int fvdbm_set_cells_eq(void* handle, const float* rho, const float* vel) {
   if (!handle || !rho || !vel) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   if (h->hp.q != 9) return fail(h, FVDBM_EINVAL, "fvdbm_set_cells_eq supports D2Q9");
   const HostPlan& hp = h->hp;
   CK(cudaSetDevice(h->device));
@@ -869,6 +904,8 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   Handle* h = static_cast<Handle*>(handle);
   if (n_steps < 0) return fail(h, FVDBM_EINVAL, "n_steps < 0");
   CK(cudaSetDevice(h->device));
+  h->in_ok = false;
+  if (n_steps == 1 && h->hp.N > 0) CK(cudaEventRecord(h->in_ready, h->stream));
   int n = n_steps;
   if (n >= kGraphSteps && h->hp.N > 0) {
     int rc = ensure_nodes(h);  // outside the capture
@@ -884,6 +921,7 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   }
   int rc = enqueue_steps(h, n);
   if (rc != FVDBM_OK) return rc;
+  h->in_ok = n_steps == 1 && h->hp.N > 0;
   h->steps_done += n_steps;
   for (size_t s = 0; s < h->active.size(); ++s)
     if (h->active[s]) h->case_steps[s] += n_steps;
@@ -918,6 +956,7 @@ int fvdbm_const_div_check_form(int32_t device, float divisor, int32_t form, uint
 int fvdbm_step_phase(void* handle, int32_t phase) {
   if (!handle) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   CK(cudaSetDevice(h->device));
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
@@ -994,9 +1033,12 @@ int fvdbm_get_cells(void* handle, float* pdf, float* rho, float* vel, float* pdf
     float* hr = rho ? static_cast<float*>(host_mapped(rho)) : nullptr;
     float* hv = vel ? static_cast<float*>(host_mapped(vel)) : nullptr;
     if ((!rho || hr) && (!vel || hv)) {
-      CK(launch_macros_ref(h->dp, h->f[h->cur ^ 1], h->d_cell_new, hr, hv, h->stream));
-      CK(cudaStreamSynchronize(h->stream));
-      return check_status(h);
+      // after a single step, beside it: its input buffer is read-only to it
+      cudaStream_t s = h->in_ok ? h->side : h->stream;
+      if (h->in_ok) CK(cudaStreamWaitEvent(h->side, h->in_ready, 0));
+      CK(launch_macros_ref(h->dp, h->f[h->cur ^ 1], h->d_cell_new, hr, hv, s, /*grid_cap=*/h->in_ok));
+      if (h->in_ok) CK(cudaStreamSynchronize(h->side));
+      return sync_and_check(h);
     }
     float* sr = h->stage;
     float* sv = h->stage + N;
@@ -1132,6 +1174,7 @@ int fvdbm_run_to_steady(void* handle, double threshold, int32_t check_every, int
                         int64_t* steps_taken, double* res_u) {
   if (!handle || !steps_taken || !res_u) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   if (check_every <= 0 || max_steps < 0) return fail(h, FVDBM_EINVAL, "check_every <= 0 or max_steps < 0");
   double r = HUGE_VAL, m = 0.0;
   int rc;
@@ -1218,6 +1261,7 @@ int scratch_address(Handle* h, float** out) {
 extern "C" int fvdbm_step_static_scratch(void* handle, int32_t n_steps) {
   if (!handle) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
   const HostPlan& hp = h->hp;
   if (n_steps < 0) return fail(h, FVDBM_EINVAL, "n_steps < 0");
   if (h->fused || h->tile || h->one)

@@ -315,8 +315,9 @@ cudaError_t launch_host_to_cells(const float* src_host, float* dst, const int* c
                                  cudaStream_t s, int q = Q);
 // D2Q9 rho [N] and vel [N][2] of a pdf buffer in reference order (either
 // may be null; both may be page-locked host memory)
+// grid_cap: at most two blocks per SM, looping over the cells
 cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_new, float* rho, float* vel,
-                              cudaStream_t s);
+                              cudaStream_t s, bool grid_cap = false);
 // D2Q13 (d2q13.cu): the staged step, the face fluxes alone, read-back macros
 cudaError_t launch13_step(const DevPlan& p, const float* fin, float* flux, float* fout, cudaStream_t s);
 cudaError_t launch13_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);

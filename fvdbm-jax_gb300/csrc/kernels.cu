@@ -733,28 +733,35 @@ __global__ void __launch_bounds__(256) k_macros(DevPlan p, const float* __restri
 __global__ void __launch_bounds__(256) k_macros_ref(DevPlan p, const float* __restrict__ f,
                                                     const int* __restrict__ cell_new, float* __restrict__ rho_o,
                                                     float* __restrict__ vel_o, int vel2) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= p.N) return;
-  float fc[Q];
-  load_cell(f, cell_new[c], fc);
-  float rho, ux, uy;
-  macros(fc, rho, ux, uy);
-  if (rho_o) rho_o[c] = rho;
-  if (vel_o) {
-    if (vel2) {
-      reinterpret_cast<float2*>(vel_o)[c] = make_float2(ux, uy);
-    } else {
-      vel_o[2 * size_t(c)] = ux;
-      vel_o[2 * size_t(c) + 1] = uy;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < p.N; c += gridDim.x * blockDim.x) {
+    float fc[Q];
+    load_cell(f, cell_new[c], fc);
+    float rho, ux, uy;
+    macros(fc, rho, ux, uy);
+    if (rho_o) rho_o[c] = rho;
+    if (vel_o) {
+      if (vel2) {
+        reinterpret_cast<float2*>(vel_o)[c] = make_float2(ux, uy);
+      } else {
+        vel_o[2 * size_t(c)] = ux;
+        vel_o[2 * size_t(c) + 1] = uy;
+      }
     }
   }
 }
 
 cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_new, float* rho, float* vel,
-                              cudaStream_t s) {
+                              cudaStream_t s, bool grid_cap) {
   if (p.N == 0) return cudaSuccess;
   const int vel2 = (reinterpret_cast<uintptr_t>(vel) & 7) == 0 ? 1 : 0;
-  k_macros_ref<<<(p.N + 255) / 256, 256, 0, s>>>(p, f, cell_new, rho, vel, vel2);
+  int grid = (p.N + 255) / 256;
+  if (grid_cap) {  // a few blocks per SM are enough to keep the host link busy
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid = std::min(grid, 2 * sms);
+  }
+  k_macros_ref<<<grid, 256, 0, s>>>(p, f, cell_new, rho, vel, vel2);
   return cudaGetLastError();
 }
 

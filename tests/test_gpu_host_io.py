@@ -1,6 +1,7 @@
 """Host I/O through the C ABI: page-locked arrays, which the device reads and
 writes directly over the host link, give the same bytes as pageable arrays,
-which go through a staging copy."""
+which go through a staging copy.  After a single step the page-locked
+rho/vel read-back runs beside the step on a second stream."""
 import numpy as np
 import pytest
 
@@ -36,7 +37,8 @@ def test_page_locked_and_pageable_io_agree(lattice):
         src[...] = pdf
         nat.check(L.fvdbm_set_state(h, nat.fptr(src), None, None, None), h)
         src[...] = 0.0  # the call has read its input
-        nat.check(L.fvdbm_step(h, 2), h)
+        nat.check(L.fvdbm_step(h, 1), h)
+        nat.check(L.fvdbm_step(h, 1), h)  # a single step: page-locked rho/vel are read beside it
         p, r, v = buf((N, Q)), buf((N,)), buf((N, 2))
         nat.check(L.fvdbm_get_cells(h, nat.fptr(p), None, None, None), h)
         nat.check(L.fvdbm_get_cells(h, None, nat.fptr(r), nat.fptr(v), None), h)
