@@ -250,7 +250,10 @@ int enqueue_steps(Handle* h, int n) {
     const float* fin = h->f[h->cur];
     float* fout = h->f[h->cur ^ 1];
     if (h->hp.q == 13) {
-      CK(launch13_step(h->dp, fin, h->flux, fout, h->stream));
+      if (h->fused)
+        CK(launch13_fused(h->dp, fin, fout, h->stream));
+      else
+        CK(launch13_step(h->dp, fin, h->flux, fout, h->stream));
     } else if (h->fnodes) {
       CK(launch_fused_nodes(with_nodes(h, h->node_cur, h->node_cur ^ 1), fin, fout, h->stream, /*pdl=*/true));
       h->node_last = h->node_cur;
@@ -437,7 +440,8 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   CR(cudaEventCreateWithFlags(&h->in_ready, cudaEventDisableTiming));
   const HostPlan& hp = h->hp;
   DevPlan& p = h->dp;
-  h->fused = hp.fusable && params->kernel != FVDBM_KERNEL_STAGED;
+  // the fused kernels take three face slots per cell (triangles)
+  h->fused = hp.fusable && hp.K == 3 && params->kernel != FVDBM_KERNEL_STAGED;
   if (params->kernel == FVDBM_KERNEL_FUSED_NODES && !(hp.fusable && hp.K == 3 && hp.stencil_first)) {
     h->err = "the in-kernel node update needs triangles (3 face slots per cell), every cell face slot "
              "naming a face of that cell, and no per-q flux scale";
@@ -446,17 +450,20 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   h->fnodes = params->kernel == FVDBM_KERNEL_FUSED_NODES ||
               (auto_family && pplan.kernel == FVDBM_KERNEL_FUSED_NODES && hp.fusable && hp.K == 3 && hp.stencil_first);
   if (hp.q == 13) {
-    // D2Q13 runs on the staged kernels (d2q13.cu)
-    if (segs || (params->kernel != FVDBM_KERNEL_AUTO && params->kernel != FVDBM_KERNEL_STAGED)) {
-      h->err = "D2Q13 runs on the staged kernels only (FVDBM_KERNEL_AUTO or FVDBM_KERNEL_STAGED), not in a batch";
+    // D2Q13 (d2q13.cu): the staged kernels, or on triangles the node kernel
+    // and one fused cell kernel
+    if (segs || (params->kernel != FVDBM_KERNEL_AUTO && params->kernel != FVDBM_KERNEL_STAGED &&
+                 params->kernel != FVDBM_KERNEL_FUSED)) {
+      h->err = "D2Q13 runs on the staged or fused kernels (FVDBM_KERNEL_AUTO, FVDBM_KERNEL_STAGED or "
+               "FVDBM_KERNEL_FUSED), not in a batch";
       return create_fail(h, FVDBM_EINVAL);
     }
-    h->fused = h->fnodes = false;
+    h->fnodes = false;
   }
   const bool want_tile = params->kernel == FVDBM_KERNEL_TILE || params->kernel == FVDBM_KERNEL_TILE_SPLIT;
-  if ((params->kernel == FVDBM_KERNEL_FUSED || want_tile) && !hp.fusable) {
-    h->err = "the fused kernels need every cell face slot to name a face of that cell "
-             "and no per-q flux scale";
+  if ((params->kernel == FVDBM_KERNEL_FUSED || want_tile) && !(hp.fusable && hp.K == 3)) {
+    h->err = "the fused kernels need triangles (3 face slots per cell), every cell face slot naming a "
+             "face of that cell, and no per-q flux scale";
     return create_fail(h, FVDBM_EINVAL);
   }
   const bool tile_possible = hp.fusable && hp.K == 3 && hp.N > 0 &&
@@ -858,7 +865,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
       CK(launch_scatter_cells(h->stage, h->f[h->cur], h->d_cell_new, hp.N, h->stream, hp.q));
     }
     read_later = mapped != nullptr;
-    if (h->fused) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
+    if (h->fused && hp.q == 9) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
     // a retired batch case keeps its state in both buffers
     for (size_t s = 0; s < h->active.size(); ++s)
       if (!h->active[s])
@@ -960,10 +967,16 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
   CK(cudaSetDevice(h->device));
   const float* fin = h->f[h->cur];
   float* fout = h->f[h->cur ^ 1];
-  if (h->hp.q == 13) {  // nodes, faces and cells in phase 2
-    if (phase == 1) return FVDBM_OK;
-    if (phase != 2) return fail(h, FVDBM_EINVAL, "phase must be 1 or 2");
-    CK(launch13_step(h->dp, fin, h->flux, fout, h->stream));
+  if (h->hp.q == 13) {  // fused: nodes in phase 1; staged: nodes, faces and cells in phase 2
+    if (phase != 1 && phase != 2) return fail(h, FVDBM_EINVAL, "phase must be 1 or 2");
+    if (phase == 1) {
+      if (h->fused) CK(launch13_nodes(h->dp, fin, h->stream));
+      return FVDBM_OK;
+    }
+    if (h->fused)
+      CK(launch13_cells(h->dp, fin, fout, h->stream));
+    else
+      CK(launch13_step(h->dp, fin, h->flux, fout, h->stream));
     h->cur ^= 1;
     h->steps_done += 1;
     return FVDBM_OK;

@@ -1,5 +1,7 @@
 // D2Q13 lattice (src/dynamics.py:77-102): the staged step (boundary nodes,
-// per-face fluxes, per-cell gather and update) and the read-back helpers
+// per-face fluxes, per-cell gather and update), the fused cell update for
+// triangle meshes (boundary nodes, then one cell kernel) and the read-back
+// helpers
 // with 13 velocities, including the (+-2, 0), (0, +-2) ones, and the
 // third-order equilibrium
 //   feq_q = (W_q rho) * (((((1 + a/C^2) + a^2/(2C^4)) - u.u/(2C^2))
@@ -201,6 +203,75 @@ __global__ void k13_gather(DevPlan p, const float* __restrict__ fin, const float
   for (int q = 0; q < Q13; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
 }
 
+// Fused cell update (k13_face + k13_gather in one pass), one thread per
+// cell: macros, feq, the flux of each of the cell's three face slots from
+// the canonical slot-0/slot-1 pair (both neighbours compute identical
+// values), the signed sum and the update, with the per-cell face slots of
+// the D2Q9 fused kernel ([Np/32][rows][32]: code, n, L*sigma, LW r and D2).
+// ((phi*v)*L)*sigma == (phi*v)*(L*sigma) exactly for sigma = +-1.
+template <int SCHEME>
+__global__ void __launch_bounds__(256) k13_fused(DevPlan p, const float* __restrict__ fin,
+                                                 float* __restrict__ fout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  const HfRows HR{3, SCHEME, 0};
+  const unsigned* hb = p.hf + size_t(i >> 5) * (HR.rows() * 32) + (i & 31);
+  float f[Q13], eq[Q13], acc[Q13];
+  load13(fin, i, f);
+  float rho, ux, uy;
+  macros13(f, rho, ux, uy);
+  feq13(rho, ux, uy, p, eq);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int code = int(__ldg(hb + HR.code(k) * 32));
+    const float nx = __uint_as_float(__ldg(hb + HR.nx(k) * 32));
+    const float ny = __uint_as_float(__ldg(hb + HR.ny(k) * 32));
+    const float Ls = __uint_as_float(__ldg(hb + HR.ls(k) * 32));
+    const int other = code >> HF_SHIFT;
+    const bool slot1 = (code & HF_SLOT1) != 0;
+    float o[Q13];
+    if (code & HF_GHOST) {
+      // ghost = m + (m - f_known)*(d_ghost/d_known), the known cell this one
+      const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
+      const float rg = __ldg(p.gh_r + other);
+#pragma unroll
+      for (int q = 0; q < Q13; ++q) {
+        const float mq = (p.node_pdf[size_t(q) * p.Mp + a] + p.node_pdf[size_t(q) * p.Mp + b]) / 2.0f;
+        o[q] = mq + (mq - f[q]) * rg;
+      }
+    } else {
+      load13(fin, other, o);
+    }
+    float r = 0.0f, D2 = 1.0f;
+    if (SCHEME == 1) {
+      r = __uint_as_float(__ldg(hb + HR.r(k) * 32));
+      D2 = __uint_as_float(__ldg(hb + HR.d2(k) * 32));
+    }
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) {
+      const float v = c_kx13[q] * nx + c_ky13[q] * ny;
+      const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
+      float phi;
+      if (SCHEME == 0) {
+        phi = v >= 0.0f ? lq : rq;
+      } else {
+        const float w = r - (v * p.dt) / D2;
+        phi = lq + (rq - lq) * w;
+      }
+      const float x = (phi * v) * Ls;
+      acc[q] = (k == 0) ? x : acc[q] + x;
+    }
+  }
+  if (p.fv) {
+    const float ia = p.inv_area[i];
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) acc[q] = acc[q] * ia;
+  }
+  float* o = fout + base13(i);
+#pragma unroll
+  for (int q = 0; q < Q13; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+}
+
 // rho [Np], vel [2][Np], feq AoSoA of a pdf buffer (read-back)
 __global__ void k13_macros(DevPlan p, const float* __restrict__ f, float* __restrict__ rho_o,
                            float* __restrict__ vel_o, float* __restrict__ feq_o) {
@@ -227,6 +298,32 @@ cudaError_t launch13_step(const DevPlan& p, const float* fin, float* flux, float
   if (p.Mc > 0) k13_nodes<<<nblk(p.Mc, 128), 128, 0, s>>>(p, fin);
   if (p.F > 0) k13_face<<<nblk(p.F, 256), 256, 0, s>>>(p, fin, flux);
   if (p.N > 0) k13_gather<<<nblk(p.N, 256), 256, 0, s>>>(p, fin, flux, fout);
+  return cudaGetLastError();
+}
+
+cudaError_t launch13_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
+  if (p.Mc > 0) k13_nodes<<<nblk(p.Mc, 128), 128, 0, s>>>(p, fin);
+  if (p.N > 0) {
+    if (p.scheme == 1)
+      k13_fused<1><<<nblk(p.N, 256), 256, 0, s>>>(p, fin, fout);
+    else
+      k13_fused<0><<<nblk(p.N, 256), 256, 0, s>>>(p, fin, fout);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch13_nodes(const DevPlan& p, const float* fin, cudaStream_t s) {
+  if (p.Mc > 0) k13_nodes<<<nblk(p.Mc, 128), 128, 0, s>>>(p, fin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch13_cells(const DevPlan& p, const float* fin, float* fout, cudaStream_t s) {
+  if (p.N > 0) {
+    if (p.scheme == 1)
+      k13_fused<1><<<nblk(p.N, 256), 256, 0, s>>>(p, fin, fout);
+    else
+      k13_fused<0><<<nblk(p.N, 256), 256, 0, s>>>(p, fin, fout);
+  }
   return cudaGetLastError();
 }
 

@@ -321,6 +321,11 @@ cudaError_t launch_macros_ref(const DevPlan& p, const float* f, const int* cell_
 // D2Q13 (d2q13.cu): the staged step, the face fluxes alone, read-back macros
 cudaError_t launch13_step(const DevPlan& p, const float* fin, float* flux, float* fout, cudaStream_t s);
 cudaError_t launch13_face_flux(const DevPlan& p, const float* f, float* flux, cudaStream_t s);
+// D2Q13 fused family (triangles): the node kernel, then one cell kernel;
+// and the two halves separately (step phases)
+cudaError_t launch13_fused(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
+cudaError_t launch13_nodes(const DevPlan& p, const float* fin, cudaStream_t s);
+cudaError_t launch13_cells(const DevPlan& p, const float* fin, float* fout, cudaStream_t s);
 cudaError_t launch13_macros(const DevPlan& p, const float* f, float* rho, float* vel, float* feq,
                             cudaStream_t s);
 // SoA [rows][Np] device order -> [N][rows] reference order

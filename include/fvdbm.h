@@ -59,9 +59,11 @@ extern "C" {
 
 /* Kernel family for the step. */
 #define FVDBM_KERNEL_AUTO 0       /* fastest family the mesh allows (FUSED_NODES from 2^18 cells,
-                                     FUSED below, STAGED when the fused kernels cannot run) */
+                                     FUSED below and for D2Q13, STAGED when the fused kernels
+                                     cannot run: not triangles, padded or foreign face slots,
+                                     per-q flux scale) */
 #define FVDBM_KERNEL_STAGED 1     /* node BC + face flux + cell gather (3 kernels) */
-#define FVDBM_KERNEL_FUSED 2      /* node BC + fused cell kernel (2 kernels) */
+#define FVDBM_KERNEL_FUSED 2      /* node BC + fused cell kernel (2 kernels; triangles) */
 #define FVDBM_KERNEL_TILE 3       /* persistent tile kernel, nodes evaluated in-tile (1 kernel) */
 #define FVDBM_KERNEL_TILE_SPLIT 4 /* node BC kernel + persistent tile kernel (2 kernels) */
 #define FVDBM_KERNEL_ONE 5        /* node and cell blocks in one launch (1 kernel) */
@@ -108,7 +110,7 @@ typedef struct fvdbm_params {
   int32_t kernel;      /* FVDBM_KERNEL_* */
   int32_t device;      /* CUDA device ordinal */
   int32_t lattice;     /* velocities: 9 (D2Q9, also when 0) or 13 (D2Q13,
-                          src/dynamics.py:77-102: staged kernels only, no
+                          src/dynamics.py:77-102: staged or fused kernels, no
                           flux-scale variant; c2, c4x2, c2x2 are then those of
                           C = 1/sqrt(2)) */
   float c6x2;          /* D2Q13: 2*C^6 with C^6 = (C*C)*((C*C)*(C*C)) */

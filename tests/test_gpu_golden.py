@@ -9,14 +9,18 @@ import goldens as G
 pytestmark = pytest.mark.gpu
 
 NOT_FUSABLE = {"mixed_quadtri_upwind", "cavity7_cc_alt_upwind"}
-D2Q13 = {"cavity7_d2q13_upwind", "channel_d2q13_lw"}  # staged kernels only
+D2Q13 = {"cavity7_d2q13_upwind", "channel_d2q13_lw"}  # staged and fused kernels
 
 
 def _cases():
     out = []
     for name in G.names():
-        kernels = ["staged", "auto"] if name in NOT_FUSABLE | D2Q13 else ["one", "tile", "tile_split", "fused", "fused_nodes",
-                                                                  "staged"]
+        if name in NOT_FUSABLE:
+            kernels = ["staged", "auto"]
+        elif name in D2Q13:
+            kernels = ["staged", "fused", "auto"]
+        else:
+            kernels = ["one", "tile", "tile_split", "fused", "fused_nodes", "staged"]
         for k in kernels:
             for order in ("none", "rcm", "morton"):
                 out.append((name, k, order))
@@ -55,16 +59,18 @@ def test_gpu_matches_reference(name, kernel, order):
 
 
 def test_d2q13_rejected_by_d2q9_only_parts():
-    """The fused families, the batch, the monitor and the warm-start
-    initialisation are D2Q9 only and say so."""
+    """The single-launch and tile families, the batch, the monitor and the
+    warm-start initialisation are D2Q9 only and say so; AUTO runs D2Q13 on
+    the fused kernels."""
     from fvdbm_jax_gb300 import Batch, Environment
     g = G.load("cavity7_d2q13_upwind")
     c, f, n = G.containers(g)
-    with pytest.raises(ValueError, match="D2Q13"):
-        Environment(c, f, n, kernel="fused").init()
+    for kernel in ("fused_nodes", "tile", "one"):
+        with pytest.raises(ValueError, match="D2Q13"):
+            Environment(c, f, n, kernel=kernel).init()
     env = Environment(c, f, n)
     env.init()
-    assert env.info()["kernel"] == 1
+    assert env.info()["kernel"] == 2
     from fvdbm_jax_gb300 import _native as nat
     with pytest.raises(nat.FvdbmError, match="D2Q9"):
         env.residual()
