@@ -515,12 +515,17 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   p.neg_one = -1.0f;
   p.q = hp.q;
   p.finite_n = hp.finite_n ? 1 : 0;
-  if (hp.q == 9) {  // (the D2Q13 kernels divide with '/')
-    CR(make_cdiv(h->device, p.c2, h->stream, &p.d_c2));
-    CR(make_cdiv(h->device, p.c4x2, h->stream, &p.d_c4x2));
-    CR(make_cdiv(h->device, p.c2x2, h->stream, &p.d_c2x2));
+  CR(make_cdiv(h->device, p.c2, h->stream, &p.d_c2));
+  CR(make_cdiv(h->device, p.c4x2, h->stream, &p.d_c4x2));
+  CR(make_cdiv(h->device, p.c2x2, h->stream, &p.d_c2x2));
+  if (hp.q == 13) {
+    CR(make_cdiv(h->device, p.c6x2, h->stream, &p.d_c6x2));
+  } else {
+    p.d_c6x2 = p.d_c2x2;  // (unused by D2Q9; keeps the conditions below uniform)
   }
-  p.cdiv_mode = (p.d_c2.ok && p.d_c4x2.ok && p.d_c2x2.ok) ? ((p.d_c2.two && p.d_c4x2.two && p.d_c2x2.two) ? 2 : 1) : 0;
+  p.cdiv_mode = (p.d_c2.ok && p.d_c4x2.ok && p.d_c2x2.ok && p.d_c6x2.ok)
+                    ? ((p.d_c2.two && p.d_c4x2.two && p.d_c2x2.two && p.d_c6x2.two) ? 2 : 1)
+                    : 0;
 
 #define UP(field, vec)                                                        \
   do {                                                                        \

@@ -12,7 +12,7 @@
 //
 // Layouts as the D2Q9 kernels: cell pdfs AoSoA [Np/32][13][32], face fluxes
 // [13][Fp], node state [13][Mp] / [Mp] / [2][Mp].
-#include "fvdbm_internal.h"
+#include "fvdbm_math.cuh"
 
 namespace fvdbm {
 
@@ -50,8 +50,63 @@ __device__ __forceinline__ void macros13(const float f[Q13], float& rho, float& 
   uy = my / r;
 }
 
+// x == 0 or 2^-30 <= |x| <= 2^30: then x^2, x*x^2, 3x*u.u and their
+// scalings by 2, 4, 8 stay in the normal range, where binary scaling commutes
+// with rounding, and every dividend is one the known-divisor check covers.
+__device__ __forceinline__ bool dom13(float x) {
+  const float a = fabsf(x);
+  return (a >= 0x1p-30f && a <= 0x1p30f) || x == 0.0f;
+}
+
+__device__ __forceinline__ float kdiv(float x, const CDiv& d, bool two) {
+  return two ? cdiv_two(x, d.zr, d.zl) : cdiv_fast(x, d.y, d.zr);
+}
+
 __device__ __forceinline__ void feq13(float rho, float ux, float uy, const DevPlan& p, float out[Q13]) {
   const float uu = ux * ux + uy * uy;
+  const float a5 = ux + uy, a6 = uy - ux;
+  if (p.cdiv_mode != 0 && dom13(ux) && dom13(uy) && dom13(a5) && dom13(a6)) {
+    // a_q = +-x or +-2x for x in (ux, uy, ux+uy, uy-ux) (a_0 = 0; the 0*u
+    // terms of the literal dot product only change the sign of a zero a,
+    // which leaves s unchanged).  Per x: t1 = x/C^2, t2 = x^2/(2C^4),
+    // t4 = x*x^2/(2C^6), t5 = 3x*u.u/(2C^4); for -x the odd ones change sign
+    // (RN(-y) = -RN(y)), for 2x they scale by 2, 4, 8, 2 exactly.  17
+    // divisions instead of 65, each the known-divisor form.
+    const bool two = p.cdiv_mode == 2;
+    const float t3 = kdiv(uu, p.d_c2x2, two);
+    const float b[4] = {ux, uy, a5, a6};
+    float t1[4], t2[4], t4[4], t5[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float x = b[j], xx = x * x;
+      t1[j] = kdiv(x, p.d_c2, two);
+      t2[j] = kdiv(xx, p.d_c4x2, two);
+      t4[j] = kdiv(x * xx, p.d_c6x2, two);
+      t5[j] = kdiv((3.0f * x) * uu, p.d_c4x2, two);
+    }
+    auto S = [t3](float a1, float a2, float a4, float a5_) {
+      float s = 1.0f + a1;
+      s = s + a2;
+      s = s - t3;
+      s = s + a4;
+      return s - a5_;
+    };
+    const float w0 = c_w13[0] * rho, w1 = c_w13[1] * rho, w5 = c_w13[5] * rho, w9 = c_w13[9] * rho;
+    out[0] = w0 * S(0.0f, 0.0f, 0.0f, 0.0f);
+    out[1] = w1 * S(t1[0], t2[0], t4[0], t5[0]);
+    out[3] = w1 * S(-t1[0], t2[0], -t4[0], -t5[0]);
+    out[2] = w1 * S(t1[1], t2[1], t4[1], t5[1]);
+    out[4] = w1 * S(-t1[1], t2[1], -t4[1], -t5[1]);
+    out[5] = w5 * S(t1[2], t2[2], t4[2], t5[2]);
+    out[7] = w5 * S(-t1[2], t2[2], -t4[2], -t5[2]);
+    out[6] = w5 * S(t1[3], t2[3], t4[3], t5[3]);
+    out[8] = w5 * S(-t1[3], t2[3], -t4[3], -t5[3]);
+    out[9] = w9 * S(2.0f * t1[0], 4.0f * t2[0], 8.0f * t4[0], 2.0f * t5[0]);
+    out[11] = w9 * S(-2.0f * t1[0], 4.0f * t2[0], -8.0f * t4[0], -2.0f * t5[0]);
+    out[10] = w9 * S(2.0f * t1[1], 4.0f * t2[1], 8.0f * t4[1], 2.0f * t5[1]);
+    out[12] = w9 * S(-2.0f * t1[1], 4.0f * t2[1], -8.0f * t4[1], -2.0f * t5[1]);
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < Q13; ++q) {
     const float a = c_kx13[q] * ux + c_ky13[q] * uy;

@@ -174,8 +174,8 @@ struct DevPlan {
   float one, neg_one;  // 1 and -1 as run-time values (paired sums of paired products)
   float c6x2;  // D2Q13: 2 C^6
   int q;       // lattice velocities: 9 or 13
-  CDiv d_c2, d_c4x2, d_c2x2;
-  int cdiv_mode;  // 2: all three two-operation forms verified, 1: five-operation, 0: neither
+  CDiv d_c2, d_c4x2, d_c2x2, d_c6x2;  // d_c6x2: D2Q13 only
+  int cdiv_mode;  // 2: the lattice's divisors' two-operation forms verified, 1: five-operation, 0: neither
   // staged faces
   const int* fs0;
   const int* fs1;

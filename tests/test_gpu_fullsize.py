@@ -140,14 +140,15 @@ def test_state_round_trip_and_midrun_write(kernel):
 
 
 @pytest.mark.parametrize("form", [5, 2])
-@pytest.mark.parametrize("which", ["c2", "c4x2", "c2x2"])
-def test_known_divisor_division_exhaustive(which, form):
+@pytest.mark.parametrize("lattice,which", [("D2Q9", "c2"), ("D2Q9", "c4x2"), ("D2Q9", "c2x2"), ("D2Q13", "c2"),
+                                           ("D2Q13", "c4x2"), ("D2Q13", "c2x2"), ("D2Q13", "c6x2")])
+def test_known_divisor_division_exhaustive(lattice, which, form):
     """Every float32 dividend: the known-divisor division (five- and
-    two-operation forms) equals IEEE x/y."""
+    two-operation forms) equals IEEE x/y, for each lattice constant."""
     import ctypes as C
-    from fvdbm_jax_gb300 import D2Q9
+    from fvdbm_jax_gb300 import D2Q9, D2Q13
     from fvdbm_jax_gb300 import _native as nat
-    y = float(getattr(D2Q9(0.6, 0.1), which))
+    y = float(getattr((D2Q9 if lattice == "D2Q9" else D2Q13)(0.6, 0.1), which))
     bad, ex = C.c_uint64(), C.c_uint32()
     nat.check(nat.lib().fvdbm_const_div_check_form(0, y, form, C.byref(bad), C.byref(ex)))
     x = np.array([ex.value], np.uint32).view(np.float32)[0]
