@@ -414,7 +414,10 @@ def run_gb300(args):
             "gpu_launches": K * info["launches_per_step"],
             "clocks": clk,
             "l2_resident": {"mcups": round(N / (res_ms / 1e3) / 1e6, 3), "ms_per_step": round(res_ms, 5),
-                            "steps": resident_steps, "note": "graph replay, no flush"},
+                            "steps": resident_steps,
+                            "frac": round(info["bytes_per_step"] / (res_ms / 1e3) / 1e9 / peak, 4),
+                            "note": "graph replay of consecutive steps, no flush (a long run's steady state); "
+                                    "frac: the step's algorithmic bytes per step time over the same peak"},
             "wall_s": round(t_wall, 3),
         }
         print(json.dumps(line), flush=True)
