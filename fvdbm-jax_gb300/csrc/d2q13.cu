@@ -35,19 +35,56 @@ __device__ __forceinline__ void load13(const float* __restrict__ f, int c, float
   for (int q = 0; q < Q13; ++q) out[q] = __ldg(b + q * 32);
 }
 
-// rho = sum_q f_q; u = (xi^T f)/rho, every product xi_q f_q kept in the fold
-// (src/dynamics.py:35-47)
+// rho = sum_q f_q; u = (xi^T f)/rho (src/dynamics.py:35-47).  For finite
+// rho every f_q is finite: the 0*f_q terms of the literal fold are +-0 and
+// leave the sum's value unchanged, +-1*f_q is +-f_q and 2*f_q is exact, so
+// the fold runs over the nonzero directions only; otherwise every product is
+// kept.
 __device__ __forceinline__ void macros13(const float f[Q13], float& rho, float& ux, float& uy) {
-  float r = f[0], mx = c_kx13[0] * f[0], my = c_ky13[0] * f[0];
+  float r = f[0];
 #pragma unroll
-  for (int q = 1; q < Q13; ++q) {
-    r = r + f[q];
-    mx = mx + c_kx13[q] * f[q];
-    my = my + c_ky13[q] * f[q];
+  for (int q = 1; q < Q13; ++q) r = r + f[q];
+  float mx, my;
+  if (fabsf(r) <= FLT_MAX) {
+    mx = ((((((f[1] - f[3]) + f[5]) - f[6]) - f[7]) + f[8]) + 2.0f * f[9]) - 2.0f * f[11];
+    my = ((((((f[2] - f[4]) + f[5]) + f[6]) - f[7]) - f[8]) + 2.0f * f[10]) - 2.0f * f[12];
+  } else {
+    mx = c_kx13[0] * f[0];
+    my = c_ky13[0] * f[0];
+#pragma unroll
+    for (int q = 1; q < Q13; ++q) {
+      mx = mx + c_kx13[q] * f[q];
+      my = my + c_ky13[q] * f[q];
+    }
   }
   rho = r;
   ux = mx / r;
   uy = my / r;
+}
+
+// v_q = xi_q . n (src/containers.py:235); for a finite normal the symmetric
+// form (+-nx, +-ny, +-(nx+ny), +-(ny-nx), +-2nx, +-2ny), whose values equal
+// the literal dot products'
+__device__ __forceinline__ void xi13_dot_n(float nx, float ny, bool finite_n, float v[Q13]) {
+  if (!finite_n) {
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) v[q] = c_kx13[q] * nx + c_ky13[q] * ny;
+    return;
+  }
+  const float s = nx + ny, d = ny - nx, x2 = 2.0f * nx, y2 = 2.0f * ny;
+  v[0] = 0.0f;
+  v[1] = nx;
+  v[2] = ny;
+  v[3] = -nx;
+  v[4] = -ny;
+  v[5] = s;
+  v[6] = d;
+  v[7] = -s;
+  v[8] = -d;
+  v[9] = x2;
+  v[10] = y2;
+  v[11] = -x2;
+  v[12] = -y2;
 }
 
 // x == 0 or 2^-30 <= |x| <= 2^30: then x^2, x*x^2, 3x*u.u and their
@@ -302,16 +339,43 @@ __global__ void __launch_bounds__(256) k13_fused(DevPlan p, const float* __restr
       r = __uint_as_float(__ldg(hb + HR.r(k) * 32));
       D2 = __uint_as_float(__ldg(hb + HR.d2(k) * 32));
     }
+    float vq[Q13];
+    xi13_dot_n(nx, ny, p.finite_n != 0, vq);
+    float w[Q13];
+    if (SCHEME == 1) {
+      // interp_q = d0/(d0+d1) - (v_q dt)/(2(d0+d1)) (src/containers.py:274);
+      // for a finite normal v_{q'} = -v_q pairs share one quotient:
+      // (-v dt)/D2 == -((v dt)/D2), and r - (-t) == r + t
+      if (p.finite_n) {
+        const float t1 = (vq[1] * p.dt) / D2, t2 = (vq[2] * p.dt) / D2, t5 = (vq[5] * p.dt) / D2;
+        const float t6 = (vq[6] * p.dt) / D2, t9 = (vq[9] * p.dt) / D2, t10 = (vq[10] * p.dt) / D2;
+        w[0] = r - (vq[0] * p.dt) / D2;
+        w[1] = r - t1;
+        w[3] = r + t1;
+        w[2] = r - t2;
+        w[4] = r + t2;
+        w[5] = r - t5;
+        w[7] = r + t5;
+        w[6] = r - t6;
+        w[8] = r + t6;
+        w[9] = r - t9;
+        w[11] = r + t9;
+        w[10] = r - t10;
+        w[12] = r + t10;
+      } else {
+#pragma unroll
+        for (int q = 0; q < Q13; ++q) w[q] = r - (vq[q] * p.dt) / D2;
+      }
+    }
 #pragma unroll
     for (int q = 0; q < Q13; ++q) {
-      const float v = c_kx13[q] * nx + c_ky13[q] * ny;
+      const float v = vq[q];
       const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
       float phi;
       if (SCHEME == 0) {
         phi = v >= 0.0f ? lq : rq;
       } else {
-        const float w = r - (v * p.dt) / D2;
-        phi = lq + (rq - lq) * w;
+        phi = lq + (rq - lq) * w[q];
       }
       const float x = (phi * v) * Ls;
       acc[q] = (k == 0) ? x : acc[q] + x;
