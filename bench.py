@@ -240,6 +240,25 @@ def cpu_oracle_rate(c, f, n, dyn, seconds, threads=0):
     return N * done / el / 1e6, threads, done, el
 
 
+def numpy_oracle_rate(c, f, n, dyn, seconds):
+    """The vectorised numpy restatement (gathers and folds over whole arrays,
+    like the reference's XLA program on the CPU): MCUPS over whole steps of
+    the same mesh until ``seconds`` elapse (at least one)."""
+    import numpy as np
+    import oracle_np as O
+    geo = O.geo_from_containers(c, f, n)
+    st = O.state_from_containers(c, n)
+    done, t0 = 0, time.perf_counter()
+    with np.errstate(all="ignore"):
+        while True:
+            st = O.step(geo, st, dyn.inv_tau, dyn.dt32)
+            done += 1
+            el = time.perf_counter() - t0
+            if el >= seconds:
+                break
+    return int(c.pdf.shape[0]) * done / el / 1e6, done, el
+
+
 def run_reference(args):
     ws, rank, local = dist_setup()
     if rank != 0:
@@ -383,9 +402,13 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, threads, done, el = cpu_oracle_rate(c, f, n, dyn, args.cpu_seconds)
+        nrate, ndone, nel = numpy_oracle_rate(c, f, n, dyn, 8.0)
         cpu = {"value": round(rate, 3), "unit": "MCUPS", "cores": threads, "kind": "port",
                "sample": f"{done} whole steps of the same {N}-cell mesh ({el:.1f}s), C restatement "
-                         f"of the reference step with OpenMP"}
+                         f"of the reference step with OpenMP",
+               "numpy": {"value": round(nrate, 3), "unit": "MCUPS",
+                         "sample": f"{ndone} whole steps ({nel:.1f}s) of the vectorised numpy restatement, "
+                                   f"whole-array gathers and folds as the reference's XLA CPU program does"}}
 
     if rank == 0:
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
