@@ -529,6 +529,14 @@ def _ws_case(spec):
                             seed=spec["seed"], mesher=True)
 
 
+def _ws_sample(job):
+    """Network input of one case (features, including the potential-flow
+    solve, and aggregation stages), with targets when rho/vel are given."""
+    from fvdbm_jax_gb300 import warmstart as WS
+    case, rho_in, rho_out, rho, vel = job
+    return WS.sample(case, rho_in, rho_out, rho, vel)
+
+
 def run_warmstart(args):
     """Learned warm start: solver-generated steady states of seeded porous
     squares train the network (on the GPU, by the library's kernels); on
@@ -552,8 +560,10 @@ def run_warmstart(args):
                 "porosity": float(rng.uniform(0.75, 0.85)), "dt": 1.0, "seed": 50_000 + i}
     specs = [spec(i) for i in range(args.train_cases + args.eval_cases)]
     t0 = time.perf_counter()
-    with cf.ProcessPoolExecutor(min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
-        allc = list(ex.map(_ws_case, specs, chunksize=4))
+    # one pool of host workers, started before the first GPU call, builds the
+    # cases and later the per-case network inputs
+    ex = cf.ProcessPoolExecutor(min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn"))
+    allc = list(ex.map(_ws_case, specs, chunksize=4))
     setup_s = time.perf_counter() - t0
     train, evalc = allc[:args.train_cases], allc[args.train_cases:]
     tspec, espec = specs[:args.train_cases], specs[args.train_cases:]
@@ -566,12 +576,13 @@ def run_warmstart(args):
     steps_t, res_t, st_t = b.run_to_steady(thr, every, cap)
     state = b.state()
     data_s = time.perf_counter() - t
-    samples = []
+    jobs = []
     for s, (case, sp) in enumerate(zip(train, tspec)):
         if st_t[s] != 1:
             continue
         rho, vel = WS.macros(b.case_state(s, state)["pdf"])
-        samples.append(WS.sample(case, sp["rho_in"], sp["rho_out"], rho, vel))
+        jobs.append((case, sp["rho_in"], sp["rho_out"], rho, vel))
+    samples = list(ex.map(_ws_sample, jobs, chunksize=4))
     b.close()
     t = time.perf_counter()
     net = WS.MPNN(seed=0)
@@ -594,12 +605,14 @@ def run_warmstart(args):
     (sp_, stp, _), plain_s, fin_p = timed(None)
     rho, vel = [], []
     t = time.perf_counter()
-    for case, sp in zip(evalc, espec):
-        y = net.predict(WS.sample(case, sp["rho_in"], sp["rho_out"]))
-        r, v = WS.untarget(y, sp["rho_in"], sp["rho_out"])
+    esamples = list(ex.map(_ws_sample, [(case, sp["rho_in"], sp["rho_out"], None, None)
+                                        for case, sp in zip(evalc, espec)]))
+    for smp, sp in zip(esamples, espec):
+        r, v = WS.untarget(net.predict(smp), sp["rho_in"], sp["rho_out"])
         rho.append(r)
         vel.append(v)
     infer_s = time.perf_counter() - t
+    ex.shutdown()
     (sw, stw, restarted), warm_s, fin_w = timed((np.concatenate(rho), np.concatenate(vel)))
     # the plain solver as a user runs it: each case alone from the uniform start
     from fvdbm_jax_gb300 import Environment
@@ -618,11 +631,14 @@ def run_warmstart(args):
     rho_p, vel_p = WS.macros(fin_p["pdf"])
     pr, pv = np.concatenate(rho), np.concatenate(vel)
     drho = np.concatenate([np.full(c[1].pdf.shape[0], s["rho_in"] - s["rho_out"]) for c, s in zip(evalc, espec)])
+    total_s = warm_s + infer_s  # the prediction is part of the warm start's cost
     line = {"metric": f"time-to-steady @{thr:g} resid, warm vs plain (held-out porous squares)",
-            "value": round(warm_s, 3), "unit": "s", "higher_is_better": False,
-            "plain_s": round(plain_s, 3), "speedup_time": round(plain_s / warm_s, 2),
+            "value": round(total_s, 3), "unit": "s", "higher_is_better": False,
+            "warm_solve_s": round(warm_s, 3),
+            "plain_s": round(plain_s, 3), "speedup_time": round(plain_s / total_s, 2),
+            "speedup_solve_only": round(plain_s / warm_s, 2),
             "plain_one_at_a_time_s": round(seq_s, 3), "plain_one_at_a_time_steps": int(seq_steps),
-            "speedup_batched_warm_vs_plain_one_at_a_time": round(seq_s / warm_s, 2),
+            "speedup_batched_warm_vs_plain_one_at_a_time": round(seq_s / total_s, 2),
             "steps_plain": int(sp_.sum()), "steps_warm": int(sw.sum()),
             "speedup_steps": round(float(sp_.sum()) / max(float(sw.sum()), 1.0), 2),
             "converged_plain": int(np.sum(stp == 1)), "converged_warm": int(np.sum(stw == 1)),

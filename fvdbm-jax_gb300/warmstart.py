@@ -31,7 +31,7 @@ import numpy as np
 
 from . import _native as nat
 
-HIDDEN, LAYERS, NFEAT, NOUT = 64, 4, 6, 3
+HIDDEN, LAYERS, NFEAT, NOUT = 64, 4, 9, 3
 # neighbourhood of each message-passing layer: mesh neighbours, then count-aware
 # bins of 16 x 16, 4 x 4 and 1 x 1 (the whole sample)
 SCALES = ("mesh", "c16", "c4", "c1")
@@ -115,12 +115,70 @@ def wall_distance(mesher, faces, nodes):
     return cKDTree(mid).query(cen)[0]
 
 
+def potential(mesher, cells, faces, nodes, rho_in: float, rho_out: float):
+    """A potential-flow estimate of the flow pattern: phi solves the cell
+    Laplacian with phi = (rho - rho_out)/(rho_in - rho_out) on open boundary
+    faces (both end nodes density nodes) and no flux through walls, face
+    conductances L/(d0 + d1) (L/d0 to a boundary face); its Green-Gauss
+    gradient points along the channels the steady flow takes.  Returns phi
+    and grad phi per cell (zeros when the mesh has no open boundary)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    fc = np.asarray(faces.stencil_cells_index, np.int64)
+    sd = np.asarray(faces.stencil_dists, np.float64)
+    L = np.asarray(faces.L, np.float64).reshape(-1)
+    fn = np.asarray(faces.nodes_index, np.int64)
+    t = np.asarray(nodes.type).reshape(-1)
+    nr = np.asarray(nodes.rho, np.float64).reshape(-1)
+    ncell = np.asarray(mesher.cell_centers).shape[0]
+    inner = (fc[:, 0] >= 0) & (fc[:, 1] >= 0)
+    bnd = ~inner
+    open_ = bnd & (t[fn[:, 0]] == 2) & (t[fn[:, 1]] == 2)
+    if not open_.any():
+        z = np.zeros(ncell)
+        return z, z, z
+    d = max(rho_in - rho_out, 1e-30)
+    phib = np.zeros(fc.shape[0])
+    phib[open_] = 0.5 * ((nr[fn[open_, 0]] - rho_out) + (nr[fn[open_, 1]] - rho_out)) / d
+    w_in = L[inner] / np.maximum(sd[inner, 0] + sd[inner, 1], 1e-30)
+    a, b = fc[inner, 0], fc[inner, 1]
+    owner = np.where(fc[:, 0] >= 0, fc[:, 0], fc[:, 1])
+    w_bd = L[open_] / np.maximum(sd[open_, 0], 1e-30)
+    ob = owner[open_]
+    diag = np.bincount(a, w_in, ncell) + np.bincount(b, w_in, ncell) + np.bincount(ob, w_bd, ncell)
+    A = sp.coo_matrix((np.concatenate([-w_in, -w_in, diag]),
+                       (np.concatenate([a, b, np.arange(ncell)]), np.concatenate([b, a, np.arange(ncell)]))),
+                      shape=(ncell, ncell)).tocsc()
+    rhs = np.bincount(ob, w_bd * phib[open_], ncell)
+    phi = spl.spsolve(A, rhs)
+    # face values: linear between the two cells, the boundary value on open
+    # faces, the owner's value on walls; then sum_k sign_k phi_f n_f L_f / A
+    pf = np.empty(fc.shape[0])
+    d0, d1 = sd[inner, 0], sd[inner, 1]
+    pf[inner] = (phi[a] * d1 + phi[b] * d0) / np.maximum(d0 + d1, 1e-30)
+    pf[bnd] = phi[owner[bnd]]
+    pf[open_] = phib[open_]
+    n = np.asarray(faces.n, np.float64)
+    cf = np.asarray(cells.face_indices, np.int64)
+    cs = np.asarray(cells.face_normals, np.float64)
+    area = np.asarray(mesher.cell_areas, np.float64).reshape(-1)
+    ok = cf >= 0
+    fi = np.where(ok, cf, 0)
+    contrib = (cs * ok)[:, :, None] * (pf[fi] * L[fi])[:, :, None] * n[fi]
+    g = contrib.sum(1) / area[:, None]
+    return phi, g[:, 0], g[:, 1]
+
+
 def features(mesher, cells, faces, nodes, rho_in: float, rho_out: float) -> np.ndarray:
+    """Per cell: centroid, wall distance, area, inlet and outlet density, and
+    the potential-flow estimate phi, grad phi."""
     cen = np.asarray(mesher.cell_centers, np.float64)
     area = np.asarray(mesher.cell_areas, np.float64).reshape(-1)
     wd = wall_distance(mesher, faces, nodes)
     n = cen.shape[0]
-    return np.stack([cen[:, 0], cen[:, 1], wd, area, np.full(n, rho_in), np.full(n, rho_out)], 1).astype(np.float32)
+    phi, gx, gy = potential(mesher, cells, faces, nodes, rho_in, rho_out)
+    return np.stack([cen[:, 0], cen[:, 1], wd, area, np.full(n, rho_in), np.full(n, rho_out), phi, -gx, -gy],
+                    1).astype(np.float32)
 
 
 def targets(rho, vel, rho_in: float, rho_out: float) -> np.ndarray:

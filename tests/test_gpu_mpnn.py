@@ -14,7 +14,7 @@ def _random_sample(n=300, seed=0):
     """A random graph with layers of both kinds: mesh-like neighbour means
     (layers 1, 2), count-aware bins on a 5 x 5 grid (layer 3) and bin means
     on a 2 x 2 grid (layer 4)."""
-    from fvdbm_jax_gb300.warmstart import Sample, _stage, grid_mean
+    from fvdbm_jax_gb300.warmstart import NFEAT, Sample, _stage, grid_mean
     rng = np.random.default_rng(seed)
     # random planar-ish graph: ring plus random chords, symmetric, mean weights
     nbr = [set() for _ in range(n)]
@@ -35,7 +35,7 @@ def _random_sample(n=300, seed=0):
     aggs = [[_stage(A)], [_stage(A)], [_stage(P5), _stage(U5)], [_stage(P2), _stage(U2)]]
     dense = [A.toarray()] * 2 + [(U5.astype(np.float32) @ P5.astype(np.float32)).toarray(),
                                  (U2.astype(np.float32) @ P2.astype(np.float32)).toarray()]
-    x = rng.standard_normal((n, 6)).astype(np.float32)
+    x = rng.standard_normal((n, NFEAT)).astype(np.float32)
     t = rng.standard_normal((n, 3)).astype(np.float32)
     return Sample(x, aggs, t), [d.astype(np.float64) for d in dense]
 
