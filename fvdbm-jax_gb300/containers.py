@@ -113,6 +113,16 @@ def _arr(x, dtype):
     return np.array(np.asarray(x), dtype=dtype, copy=True)
 
 
+def _rows(a, n: int):
+    """a as [n, k]; a 2-D array keeps its k (also when n is 0, where
+    reshape(0, -1) has no answer)."""
+    if a.ndim == 2 and a.shape[0] == n:
+        return a
+    if n == 0:
+        return a.reshape(0, a.shape[-1] if a.ndim >= 2 else 1)
+    return a.reshape(n, -1)
+
+
 def from_any(cells, faces, nodes, dynamics=None):
     """Copy reference (or these) containers into fresh host containers; the
     originals are never modified.
@@ -131,8 +141,8 @@ def from_any(cells, faces, nodes, dynamics=None):
     c.rho = _arr(cells.rho, F32).reshape(N, 1)
     c.vel = _arr(cells.vel, F32).reshape(N, 2)
     c.pdf_eq = _arr(cells.pdf_eq, F32).reshape(N, Q)
-    c.face_indices = _arr(cells.face_indices, I32).reshape(N, -1)
-    c.face_normals = _arr(cells.face_normals, I32).reshape(N, -1)
+    c.face_indices = _rows(_arr(cells.face_indices, I32), N)
+    c.face_normals = _rows(_arr(cells.face_normals, I32), N)
     for extra in ("centroids", "areas"):
         if getattr(cells, extra, None) is not None:
             setattr(c, extra, _arr(getattr(cells, extra), F32))
@@ -156,6 +166,6 @@ def from_any(cells, faces, nodes, dynamics=None):
     n.rho = _arr(nodes.rho, F32).reshape(P, 1)
     n.vel = _arr(nodes.vel, F32).reshape(P, 2)
     n.type = _arr(nodes.type, I32).reshape(P, 1)
-    n.cells_index = _arr(nodes.cells_index, I32).reshape(P, -1)
-    n.cell_dists = _arr(nodes.cell_dists, F32).reshape(P, -1)
+    n.cells_index = _rows(_arr(nodes.cells_index, I32), P)
+    n.cell_dists = _rows(_arr(nodes.cell_dists, F32), P)
     return c, f, n
