@@ -284,12 +284,15 @@ int enqueue_steps(Handle* h, int n) {
   return FVDBM_OK;
 }
 
+std::string status_message(int st) {
+  return "device status " + std::to_string(st) +
+         ": a bounded wait in a step kernel (tile kernel, or node blocks of a single-launch step) gave up";
+}
+
 int check_status(Handle* h) {
   int st = 0;
   CK(cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (st != 0)
-    return fail(h, FVDBM_EDEVICE, "device status " + std::to_string(st) +
-                                      ": a bounded wait in the tile kernel gave up");
+  if (st != 0) return fail(h, FVDBM_EDEVICE, status_message(st));
   return FVDBM_OK;
 }
 
@@ -298,9 +301,7 @@ int check_status(Handle* h) {
 int sync_and_check(Handle* h) {
   CK(cudaMemcpyAsync(h->status_host, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (*h->status_host != 0)
-    return fail(h, FVDBM_EDEVICE, "device status " + std::to_string(*h->status_host) +
-                                      ": a bounded wait in the tile kernel gave up");
+  if (*h->status_host != 0) return fail(h, FVDBM_EDEVICE, status_message(*h->status_host));
   return FVDBM_OK;
 }
 
