@@ -58,7 +58,7 @@ class Info(C.Structure):
 _LIB = None
 EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", "fvdbm_get_cells", "fvdbm_get_nodes",
            "fvdbm_get_face_fluxes", "fvdbm_sync", "fvdbm_stream", "fvdbm_get_info",
-           "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check", "fvdbm_const_div_check_form",
+           "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check", "fvdbm_const_div_check_form", "fvdbm_wait_selftest",
            "fvdbm_step_static_scratch", "fvdbm_residual", "fvdbm_run_to_steady",
            "fvdbm_batch_create", "fvdbm_batch_config", "fvdbm_batch_residual", "fvdbm_batch_set_active",
            "fvdbm_batch_run_to_steady", "fvdbm_set_cells_eq",
@@ -122,6 +122,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_destroy.argtypes = [vp]
     L.fvdbm_abi_version.restype = C.c_int
     L.fvdbm_const_div_check.argtypes = [C.c_int32, C.c_float, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
+    L.fvdbm_wait_selftest.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
     L.fvdbm_const_div_check_form.argtypes = [C.c_int32, C.c_float, C.c_int32, C.POINTER(C.c_uint64),
                                              C.POINTER(C.c_uint32)]
     for name in EXPORTS:

@@ -941,6 +941,29 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   return FVDBM_OK;
 }
 
+int fvdbm_wait_selftest(int32_t device, int32_t flag_set, int32_t iterations, int32_t* status) {
+  if (!status || iterations < 1 || iterations > (1 << 24)) return FVDBM_EINVAL;
+  cudaError_t e = cudaSetDevice(device);
+  cudaStream_t s = nullptr;
+  int* d = nullptr;  // [0] flag, [1] status
+  int host[2] = {flag_set ? 1 : 0, 0};
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&d, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d, host, 2 * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = launch_wait_selftest(d, iterations, d + 1, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, d, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d) cudaFree(d);
+  if (s) cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = std::string("fvdbm_wait_selftest: ") + cudaGetErrorString(e);
+    return FVDBM_ECUDA;
+  }
+  *status = host[1];
+  return FVDBM_OK;
+}
+
 int fvdbm_const_div_check(int32_t device, float divisor, uint64_t* mismatches,
                           uint32_t* first_mismatch) {
   return fvdbm_const_div_check_form(device, divisor, 5, mismatches, first_mismatch);

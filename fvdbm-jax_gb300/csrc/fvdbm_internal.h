@@ -310,6 +310,8 @@ cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* ce
                                  cudaStream_t s, int q = Q);
 cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cell_new, int N,
                                 cudaStream_t s, int q = Q);
+// the bounded-wait self-test (fvdbm_wait_selftest)
+cudaError_t launch_wait_selftest(const int* flag, int iters, int* status, cudaStream_t s);
 // the scatter reading page-locked host memory directly (src 16-byte aligned)
 cudaError_t launch_host_to_cells(const float* src_host, float* dst, const int* cell_new, int N,
                                  cudaStream_t s, int q = Q);

@@ -12,6 +12,25 @@
 
 namespace fvdbm {
 
+// Acquire load of a flag written by other blocks of the same launch.
+__device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+  return v;
+}
+
+// Bounded wait (one thread): spin until *ctr >= target with an acquire load,
+// sleeping ns between polls, at most iters polls.  Returns false when the
+// limit ran out; the caller then records STATUS_WAIT_TIMEOUT and skips the
+// work that needed the wait, so the launch still ends.
+__device__ __forceinline__ bool wait_at_least(const int* ctr, int target, int iters, unsigned ns) {
+  for (int it = 0; it < iters; ++it) {
+    if (ld_acquire_gpu(ctr) >= target) return true;
+    __nanosleep(ns);
+  }
+  return false;
+}
+
 // Macros of a node-stencil cell for the next step's node kernel:
 // rho, ux, uy, f_q - feq_q (src/containers.py:93-105,388-390).
 __device__ __forceinline__ void record_stencil(const DevPlan& p, int i, const float fn[Q]) {
@@ -426,12 +445,7 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
   fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
 }
 
-// Acquire load of a flag written by other blocks of the same launch.
-__device__ __forceinline__ int ld_acquire_gpu(const int* ptr) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
-  return v;
-}
+
 
 // The fused cell kernel with the next step's boundary-node update in the same
 // launch.  The node-stencil cells come first (cell blocks [0, R) record their
@@ -458,14 +472,7 @@ __global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __r
   if (b >= node_at && b < node_at + p.NB) {
     grid_dep_wait();  // counters and set values of the previous launch
     if (threadIdx.x == 0) {
-      int ok = 0;
-      for (int it = 0; it < (1 << 22); ++it) {
-        if (ld_acquire_gpu(&ctr[0]) >= R) {
-          ok = 1;
-          break;
-        }
-        __nanosleep(128);
-      }
+      const bool ok = wait_at_least(&ctr[0], R, 1 << 22, 128);
       if (!ok) atomicExch(p.status, STATUS_WAIT_TIMEOUT);
       s_ok = ok;
     }
@@ -587,14 +594,7 @@ __global__ void __launch_bounds__(256) k_step(DevPlan p, const float* __restrict
     load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
     if (__ldg(p.cblk_ghost + cb)) {
       if (threadIdx.x == 0) {
-        int ok = 0;
-        for (int it = 0; it < (1 << 24); ++it) {
-          if (ld_acquire_gpu(&ctr[1]) >= p.NB) {
-            ok = 1;
-            break;
-          }
-          __nanosleep(64);
-        }
+        const bool ok = wait_at_least(&ctr[1], p.NB, 1 << 24, 64);
         if (!ok) atomicExch(p.status, STATUS_WAIT_TIMEOUT);
         s_ok = ok;
       }
@@ -817,6 +817,14 @@ __global__ void k_soa_to_aos(const float* __restrict__ src, float* __restrict__ 
   if (c >= N) return;
   const int d = cell_new[c];
   for (int q = 0; q < rows; ++q) dst[size_t(c) * rows + q] = src[size_t(q) * Np + d];
+}
+
+// Self-test of the bounded wait the step kernels use: one thread waits for
+// *flag >= 1 at most iters polls; a wait that runs out records
+// STATUS_WAIT_TIMEOUT in *status, as the step kernels do.
+__global__ void k_wait_selftest(const int* flag, int iters, int* status) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !wait_at_least(flag, 1, iters, 128))
+    atomicExch(status, STATUS_WAIT_TIMEOUT);
 }
 
 // Exhaustive check of cdiv (five-operation form, or the two-operation form
@@ -1068,6 +1076,11 @@ cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* ce
     k_aos_to_cells<13><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
   else
     k_aos_to_cells<Q><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wait_selftest(const int* flag, int iters, int* status, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(flag, iters, status);
   return cudaGetLastError();
 }
 

@@ -177,6 +177,16 @@ int fvdbm_get_nodes(void *handle, float *pdf, float *rho, float *vel);
  * (src/containers.py:205-213).  flux [F][9]. */
 int fvdbm_get_face_fluxes(void *handle, float *flux);
 
+/* Self-test of the bounded wait that the step kernels use (the node blocks
+ * of the single-launch step wait for the blocks that record the stencil
+ * macros): one device thread waits for a flag, set beforehand when flag_set
+ * is nonzero and never set otherwise, polling at most `iterations` times
+ * (1 .. 2^24, each poll followed by a ~128 ns sleep).  *status receives the
+ * device status word: 0, or FVDBM_STATUS_WAIT_TIMEOUT when the wait ran out;
+ * the context stays usable either way.  No counterpart in the reference. */
+#define FVDBM_STATUS_WAIT_TIMEOUT 1
+int fvdbm_wait_selftest(int32_t device, int32_t flag_set, int32_t iterations, int32_t *status);
+
 /* Self-test of the division by a known divisor that the kernels use for the
  * lattice constants C^2, 2C^4 and 2C^2: counts, over all 2^32 float32
  * dividends, those whose quotient differs in value from IEEE x / divisor on
