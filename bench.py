@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--threshold", type=float, default=1e-6)
     ap.add_argument("--check-every", type=int, default=100)
-    ap.add_argument("--step-cap", type=int, default=20000)
+    ap.add_argument("--step-cap", type=int, default=None,
+                    help="per-case step cap (default: 20000 for batch, 100000 for warmstart)")
     # --workload warmstart: learned warm start against the uniform start
     ap.add_argument("--train-cases", type=int, default=256)
     ap.add_argument("--eval-cases", type=int, default=64)
@@ -471,7 +472,7 @@ def run_batch(args):
     torch.cuda.set_device(local)
     setup_s = time.perf_counter() - t0
     cells = np.array([d["cells"] for d in desc], np.int64)
-    thr, every, cap = args.threshold, args.check_every, args.step_cap
+    thr, every, cap = args.threshold, args.check_every, args.step_cap or 20000
 
     b = Batch([(c, f, n) for _, c, f, n in suite], device=local)
     b.init()
@@ -567,7 +568,7 @@ def run_warmstart(args):
     setup_s = time.perf_counter() - t0
     train, evalc = allc[:args.train_cases], allc[args.train_cases:]
     tspec, espec = specs[:args.train_cases], specs[args.train_cases:]
-    thr, every, cap = args.threshold, args.check_every, args.step_cap
+    thr, every, cap = args.threshold, args.check_every, args.step_cap or 100_000
 
     # training data: the solver's own steady states
     t = time.perf_counter()
