@@ -367,19 +367,33 @@ __global__ void __launch_bounds__(256) k13_fused(DevPlan p, const float* __restr
         for (int q = 0; q < Q13; ++q) w[q] = r - (vq[q] * p.dt) / D2;
       }
     }
+    float phi[Q13];
 #pragma unroll
     for (int q = 0; q < Q13; ++q) {
-      const float v = vq[q];
       const float lq = slot1 ? o[q] : f[q], rq = slot1 ? f[q] : o[q];
-      float phi;
-      if (SCHEME == 0) {
-        phi = v >= 0.0f ? lq : rq;
-      } else {
-        phi = lq + (rq - lq) * w[q];
-      }
-      const float x = (phi * v) * Ls;
+      phi[q] = (SCHEME == 0) ? (vq[q] >= 0.0f ? lq : rq) : lq + (rq - lq) * w[q];
+    }
+#if FVDBM_PAIRED
+    // paired products; a sum that takes one is the multiply-add acc*one + x
+    const float2 L2 = make_float2(Ls, Ls), one2 = make_float2(p.one, p.one);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const float2 x = mul2(mul2(make_float2(phi[2 * j], phi[2 * j + 1]), make_float2(vq[2 * j], vq[2 * j + 1])), L2);
+      const float2 a = (k == 0) ? x : fold2(make_float2(acc[2 * j], acc[2 * j + 1]), one2, x);
+      acc[2 * j] = a.x;
+      acc[2 * j + 1] = a.y;
+    }
+    {
+      const float x = (phi[12] * vq[12]) * Ls;
+      acc[12] = (k == 0) ? x : acc[12] + x;
+    }
+#else
+#pragma unroll
+    for (int q = 0; q < Q13; ++q) {
+      const float x = (phi[q] * vq[q]) * Ls;
       acc[q] = (k == 0) ? x : acc[q] + x;
     }
+#endif
   }
   if (p.fv) {
     const float ia = p.inv_area[i];
@@ -387,8 +401,24 @@ __global__ void __launch_bounds__(256) k13_fused(DevPlan p, const float* __restr
     for (int q = 0; q < Q13; ++q) acc[q] = acc[q] * ia;
   }
   float* o = fout + base13(i);
+#if FVDBM_PAIRED
+  // f + dt*(inv_tau*(eq - f) - acc), pairwise
+  const float2 it2 = make_float2(p.inv_tau, p.inv_tau), dt2 = make_float2(p.dt, p.dt);
+  const float2 one2 = make_float2(p.one, p.one), m12 = make_float2(p.neg_one, p.neg_one);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const float2 f2 = make_float2(f[2 * j], f[2 * j + 1]);
+    const float2 d = fold2(f2, m12, make_float2(eq[2 * j], eq[2 * j + 1]));
+    const float2 u = fold2(make_float2(acc[2 * j], acc[2 * j + 1]), m12, mul2(it2, d));
+    const float2 r = fold2(f2, one2, mul2(dt2, u));
+    o[(2 * j) * 32] = r.x;
+    o[(2 * j + 1) * 32] = r.y;
+  }
+  o[12 * 32] = f[12] + p.dt * (p.inv_tau * (eq[12] - f[12]) - acc[12]);
+#else
 #pragma unroll
   for (int q = 0; q < Q13; ++q) o[q * 32] = f[q] + p.dt * (p.inv_tau * (eq[q] - f[q]) - acc[q]);
+#endif
 }
 
 // rho [Np], vel [2][Np], feq AoSoA of a pdf buffer (read-back)
