@@ -502,7 +502,7 @@ def run_batch(args):
     work = sum_over_ranks(float(np.sum(cells * steps_b)), ws, local)
     work_p = sum_over_ranks(float(np.sum(cells * steps_p)), ws, local)
     same = sum_over_ranks(float(not np.array_equal(steps_b, steps_p)), ws, local) == 0
-    counts = [sum_over_ranks(float(np.sum(st_b == k)), ws, local) for k in (1, 0, 2)]
+    counts = [sum_over_ranks(float(np.sum(st_b == k)), ws, local) for k in (1, 0, 2, 3, 4)]
     all_cells = sum_over_ranks(float(cells.sum()), ws, local)
     if rank != 0:
         return
@@ -513,6 +513,7 @@ def run_batch(args):
             "plain_mcups": round(work_p / plain_s / 1e6, 1),
             "same_steps": bool(same),
             "converged": int(counts[0]), "capped": int(counts[1]), "nonfinite": int(counts[2]),
+            "frozen": int(counts[3]), "stalled": int(counts[4]),
             "steps_median": int(np.median(steps_b)), "n_gpus": ws, "scaling": "strong", "dtype": "f32",
             "data": "synthetic",
             "autotune": tune,

@@ -127,7 +127,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
                                              C.POINTER(C.c_uint32)]
     for name in EXPORTS:
         getattr(L, name)
-    if L.fvdbm_abi_version() != 3:
+    if L.fvdbm_abi_version() != 4:
         raise RuntimeError("libfvdbm ABI version mismatch")
     _LIB = L
     return L
@@ -145,10 +145,20 @@ class FvdbmError(RuntimeError):
     pass
 
 
+class NonFiniteError(FvdbmError, FloatingPointError):
+    """The state turned non-finite (``FVDBM_ENONFINITE``): the run diverged."""
+
+
+ENONFINITE = -5
+# per-case outcome of fvdbm_batch_run_to_steady
+CASE_CAPPED, CASE_CONVERGED, CASE_NONFINITE, CASE_FROZEN, CASE_STALLED = 0, 1, 2, 3, 4
+
+
 def check(rc: int, handle=None):
     if rc != 0:
         msg = lib().fvdbm_last_error(handle)
-        raise FvdbmError(f"libfvdbm error {rc}: {msg.decode() if msg else ''}")
+        cls = NonFiniteError if rc == ENONFINITE else FvdbmError
+        raise cls(f"libfvdbm error {rc}: {msg.decode() if msg else ''}")
 
 
 def c_contig(a, dtype):

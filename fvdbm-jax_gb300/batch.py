@@ -138,7 +138,9 @@ class Batch:
     def run_to_steady(self, threshold: float = 1e-6, check_every: int = 100, max_steps=1_000_000):
         """Step until every case's residual is below ``threshold`` (or NaN,
         or its step cap).  Returns per-case (steps, res_u, status) with status
-        1 = converged, 0 = step cap, 2 = non-finite."""
+        1 = converged, 0 = step cap, 2 = non-finite, 3 = frozen (residual
+        exactly 0 before the threshold: the float32 state stopped changing),
+        4 = stalled (no new residual minimum in 50 checks)."""
         S = self.n_cases
         cap = np.ascontiguousarray(np.broadcast_to(np.asarray(max_steps, np.int64), (S,)))
         steps, res, status = np.empty(S, np.int64), np.empty(S, np.float64), np.empty(S, np.int32)

@@ -810,13 +810,13 @@ int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_ever
   if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
   if (check_every <= 0) return fail(h, FVDBM_EINVAL, "check_every <= 0");
   const int S = h->hp.S;
-  std::vector<int32_t> act(S);
-  std::vector<double> r(S, HUGE_VAL), m(S);
+  std::vector<int32_t> act(S), since_best(S, 0);
+  std::vector<double> r(S, HUGE_VAL), m(S), best(S, HUGE_VAL);
   for (int s = 0; s < S; ++s) {
     if (max_steps[s] < 0) return fail(h, FVDBM_EINVAL, "max_steps < 0");
     steps[s] = 0;
     res_u[s] = HUGE_VAL;
-    status[s] = 0;
+    status[s] = FVDBM_CASE_CAPPED;
     act[s] = max_steps[s] > 0;
   }
   int rc = fvdbm_batch_set_active(h, act.data());
@@ -838,11 +838,23 @@ int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_ever
     for (int s = 0; s < S; ++s) {
       if (!act[s]) continue;
       res_u[s] = r[s];
+      if (r[s] < best[s]) {
+        best[s] = r[s];
+        since_best[s] = 0;
+      } else {
+        ++since_best[s];
+      }
       if (std::isnan(r[s])) {
-        status[s] = 2;
+        status[s] = FVDBM_CASE_NONFINITE;
+        act[s] = 0;
+      } else if (r[s] == 0.0) {
+        status[s] = FVDBM_CASE_FROZEN;
         act[s] = 0;
       } else if (r[s] < threshold) {
-        status[s] = 1;
+        status[s] = FVDBM_CASE_CONVERGED;
+        act[s] = 0;
+      } else if (since_best[s] >= FVDBM_STALL_CHECKS) {
+        status[s] = FVDBM_CASE_STALLED;
         act[s] = 0;
       } else if (steps[s] >= max_steps[s]) {
         act[s] = 0;
@@ -1232,6 +1244,9 @@ int fvdbm_run_to_steady(void* handle, double threshold, int32_t check_every, int
   }
   *steps_taken = taken;
   *res_u = r;
+  if (std::isnan(r))
+    return fail(h, FVDBM_ENONFINITE, "fvdbm_run_to_steady: the residual turned NaN after " + std::to_string(taken) +
+                                         " steps (a cell's rho or u is not finite: the run diverged)");
   return FVDBM_OK;
 }
 
@@ -1277,22 +1292,60 @@ namespace {
 
 constexpr int kScratchDevices = 64;
 std::mutex g_scratch_mu;
+// Per device: the array's address and the id of the CUDA context it was
+// looked up in (0 when the id could not be read).
 float* g_scratch_addr[kScratchDevices] = {};
+unsigned long long g_scratch_ctx[kScratchDevices] = {};
 
-// Device address of the scratch array on h's device (current on entry),
-// looked up on the first call for that device.
+// Id of the current CUDA context (unique for the life of the process, so a
+// context re-created after cudaDeviceReset gets a new one), through the
+// driver entry points the runtime hands out (no link-time dependency on the
+// driver library); 0 when unavailable.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa{}, qb{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<GetCurrent>(a);
+      get_id = reinterpret_cast<GetId>(b);
+    }
+    cudaGetLastError();
+    looked_up = true;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of the scratch array on h's device (current on entry).
+// Set-up once per device and context: the first call on a device (and the
+// first call after the device's context was re-created, e.g. by
+// cudaDeviceReset) looks the address up with cudaGetSymbolAddress; later
+// calls reuse it.  When the context id cannot be read, every call looks the
+// address up again.
 int scratch_address(Handle* h, float** out) {
   if (h->device < 0 || h->device >= kScratchDevices)
     return fail(h, FVDBM_EINVAL, "fvdbm_step_static_scratch: device index " + std::to_string(h->device) +
                                      " out of range");
   std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (!g_scratch_addr[h->device]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch_addr[h->device] || ctx == 0 || g_scratch_ctx[h->device] != ctx) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_face_flux_scratch);
     if (e != cudaSuccess)
       return fail(h, FVDBM_ECUDA, std::string("cudaGetSymbolAddress(face flux scratch): ") +
                                       cudaGetErrorString(e));
     g_scratch_addr[h->device] = static_cast<float*>(p);
+    g_scratch_ctx[h->device] = ctx;
   }
   *out = g_scratch_addr[h->device];
   return FVDBM_OK;
@@ -1306,10 +1359,10 @@ extern "C" int fvdbm_step_static_scratch(void* handle, int32_t n_steps) {
   h->in_ok = false;
   const HostPlan& hp = h->hp;
   if (n_steps < 0) return fail(h, FVDBM_EINVAL, "n_steps < 0");
-  if (h->fused || h->tile || h->one)
+  if (h->fused || h->tile || h->one || h->batch)
     return fail(h, FVDBM_EINVAL,
-                "fvdbm_step_static_scratch steps the staged kernels only: create the handle with "
-                "FVDBM_KERNEL_STAGED");
+                "fvdbm_step_static_scratch steps the staged kernels of a single mesh only: create the "
+                "handle with fvdbm_create and FVDBM_KERNEL_STAGED (not a batch)");
   if (hp.q != 9) return fail(h, FVDBM_EINVAL, "fvdbm_step_static_scratch steps D2Q9 meshes only");
   if (hp.Fp > FVDBM_STATIC_SCRATCH_MAX_FACES)
     return fail(h, FVDBM_EINVAL,

@@ -176,7 +176,14 @@ class Environment:
 
     # ------------------------------------------------------------------
     def step(self, n_steps: int = 1):
-        """``n_steps`` FVDBM steps (``src/environment.py:55-65``); returns self."""
+        """``n_steps`` FVDBM steps (``src/environment.py:55-65``); returns self.
+
+        Unlike the reference's jitted ``step``, which returns a new pytree and
+        leaves the old ``env`` as it was, this advances ``self`` in place (the
+        state lives on the device) and returns it: ``env = env.step()`` reads
+        the same, but after ``env2 = env.step()`` both names refer to the
+        stepped environment.  Keep an earlier state with ``to_pickle`` or by
+        copying ``env.cells.pdf`` / ``env.nodes.*`` before stepping."""
         if self._h is None:
             self.init()
         nat.check(nat.lib().fvdbm_step(self._h, int(n_steps)), self._h)
@@ -197,15 +204,19 @@ class Environment:
 
     def run_to_steady(self, threshold: float = 1e-6, check_every: int = 100, max_steps: int = 1_000_000):
         """Step until the residual falls below ``threshold`` (checked every
-        ``check_every`` steps) or ``max_steps``; returns (steps, res_u)."""
+        ``check_every`` steps) or ``max_steps``; returns (steps, res_u).
+        res_u == 0 means the float32 state froze (no cell's velocity changed
+        over the last check).  A NaN residual (the run diverged) raises
+        ``NonFiniteError`` after the steps taken are recorded."""
         if self._h is None:
             self.init()
         n, r = C.c_int64(), C.c_double()
-        nat.check(nat.lib().fvdbm_run_to_steady(self._h, float(threshold), int(check_every), int(max_steps),
-                                                C.byref(n), C.byref(r)), self._h)
+        rc = nat.lib().fvdbm_run_to_steady(self._h, float(threshold), int(check_every), int(max_steps),
+                                           C.byref(n), C.byref(r))
         if n.value:
             self._steps += n.value
             self._version += 1
+        nat.check(rc, self._h)
         return n.value, r.value
 
     def sync(self):

@@ -335,10 +335,14 @@ class Mesher:
         np.savetxt(buf, np.hstack([vel, np.zeros((N, 1))]), fmt="%.9g")
         buf.write("SCALARS Density double 1\nLOOKUP_TABLE default\n")
         np.savetxt(buf, rho[:, None], fmt="%.9g")
-        for flag, name, arr in ((save_f, "pdf", "pdf"), (save_feq, "feq", "pdf_eq")):
-            if flag:
-                a = np.asarray(getattr(env.cells, arr), dtype=np.float64)
-                buf.write(f"FIELD FieldData 1\n{name} {a.shape[1]} {N} double\n")
+        # pdf and feq are cell arrays of 9 (13) components: one FIELD block
+        # holding each requested array, as VTK's legacy writer emits them
+        extra = [(name, np.asarray(getattr(env.cells, arr), dtype=np.float64).reshape(N, -1))
+                 for flag, name, arr in ((save_f, "pdf", "pdf"), (save_feq, "feq", "pdf_eq")) if flag]
+        if extra:
+            buf.write(f"FIELD FieldData {len(extra)}\n")
+            for name, a in extra:
+                buf.write(f"{name} {a.shape[1]} {N} double\n")
                 np.savetxt(buf, a, fmt="%.9g")
         path = f"{filename}.vtk"
         with open(path, "w") as fh:

@@ -492,8 +492,8 @@ def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, st
     case whose residual after ``stall_checks`` checks is not below
     ``stall_factor`` times its value ``stall_checks`` checks earlier restarts
     from the uniform state feq(1, 0).  Returns per-case steps (including the
-    steps before a restart), status (1 converged, 0 cap, 2 non-finite) and the
-    restart flags."""
+    steps before a restart), status (1 converged, 0 cap, 2 non-finite, 3
+    frozen: residual exactly 0 before the threshold) and the restart flags."""
     S = batch.n_cases
     if init is not None:
         batch.set_cells_eq(*init)
@@ -514,6 +514,8 @@ def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, st
             hist[s].append(r[s])
             if np.isnan(r[s]):
                 status[s], active[s] = 2, False
+            elif r[s] == 0.0:
+                status[s], active[s] = 3, False
             elif r[s] < threshold:
                 status[s], active[s] = 1, False
             elif steps[s] >= cap:

@@ -31,13 +31,15 @@
 extern "C" {
 #endif
 
-#define FVDBM_ABI_VERSION 3
+#define FVDBM_ABI_VERSION 4
 
 #define FVDBM_OK 0
 #define FVDBM_EINVAL (-1)  /* invalid argument or inconsistent mesh */
 #define FVDBM_ECUDA (-2)   /* CUDA runtime error */
 #define FVDBM_ENOMEM (-3)  /* allocation failed */
 #define FVDBM_EDEVICE (-4) /* device-side status word set */
+#define FVDBM_ENONFINITE (-5) /* fvdbm_run_to_steady: the state turned non-finite
+                                 (NaN residual): the run diverged */
 
 /* Faces.flux_scheme (src/containers.py:197-203) */
 #define FVDBM_UPWIND 0
@@ -234,10 +236,15 @@ int fvdbm_abi_version(void);
  * are bitwise reproducible.  Synchronises the handle's stream. */
 int fvdbm_residual(void *handle, double *res_u, double *mass);
 
-/* Steps in chunks of check_every until res_u < threshold (or is NaN), or
- * max_steps steps were taken.  steps_taken and res_u receive the outcome
- * (res_u of the last check).  The first residual snapshot is taken before
- * the first chunk when none is current. */
+/* Steps in chunks of check_every until res_u < threshold, or max_steps
+ * steps were taken.  steps_taken and res_u receive the outcome (res_u of the
+ * last check).  The first residual snapshot is taken before the first chunk
+ * when none is current.  res_u == 0 means that no cell's velocity changed
+ * over the last chunk: the float32 state is frozen (a fixed point of the
+ * float32 step, which it will not leave), whether or not the flow developed;
+ * the run stops there.  A NaN residual (a cell's rho or u not finite: the
+ * run diverged) stops the run and returns FVDBM_ENONFINITE, with
+ * steps_taken and res_u filled. */
 int fvdbm_run_to_steady(void *handle, double threshold, int32_t check_every, int64_t max_steps,
                         int64_t *steps_taken, double *res_u);
 
@@ -265,11 +272,26 @@ int fvdbm_batch_residual(void *handle, double *res_u, double *mass);
  * current state in both buffers and are skipped by the step.  [n_cases]. */
 int fvdbm_batch_set_active(void *handle, const int32_t *active);
 
-/* Steps every active case, checking the residuals every check_every steps;
- * a case retires when its residual falls below threshold (status 1), turns
- * NaN (status 2) or when it has taken max_steps[s] steps (status 0).
+/* Steps every active case, checking the residuals every check_every steps.
+ * A case retires with
+ *   FVDBM_CASE_CONVERGED  its residual fell below threshold (and is not 0),
+ *   FVDBM_CASE_NONFINITE  its residual turned NaN (the case diverged),
+ *   FVDBM_CASE_FROZEN     its residual is exactly 0: no cell's velocity
+ *                         changed over the last check interval, a fixed
+ *                         point of the float32 step reached before the
+ *                         residual passed the threshold (typically a flow
+ *                         that float32 keeps from developing),
+ *   FVDBM_CASE_STALLED    its residual set no new minimum in
+ *                         FVDBM_STALL_CHECKS consecutive checks,
+ *   FVDBM_CASE_CAPPED     it took max_steps[s] steps.
  * Returns when no case is active.  steps [n_cases] = steps each case took,
  * res_u = its last residual, status as above.  Arrays are [n_cases]. */
+#define FVDBM_CASE_CAPPED 0
+#define FVDBM_CASE_CONVERGED 1
+#define FVDBM_CASE_NONFINITE 2
+#define FVDBM_CASE_FROZEN 3
+#define FVDBM_CASE_STALLED 4
+#define FVDBM_STALL_CHECKS 50
 int fvdbm_batch_run_to_steady(void *handle, double threshold, int32_t check_every,
                               const int64_t *max_steps, int64_t *steps, double *res_u,
                               int32_t *status);
@@ -289,12 +311,13 @@ int fvdbm_batch_run_to_steady(void *handle, double threshold, int32_t check_ever
  * device's memory (JAX/XLA preallocates most of it by default, so the
  * reference's own process has little left) or because a cudaMalloc or
  * cudaFree there would stall the device (cudaFree synchronises it).
- * Only handles created with FVDBM_KERNEL_STAGED (or that the fused kernels
- * refused) are accepted; meshes whose padded face count exceeds
- * FVDBM_STATIC_SCRATCH_MAX_FACES are rejected with FVDBM_EINVAL and a
- * message, before any work is queued.  The first call on a device looks up
- * the array's device address (once per device, under a lock); make that
- * first call before any stream capture.  Every call on a device shares the
+ * Only single-mesh handles created with FVDBM_KERNEL_STAGED (or that the
+ * fused kernels refused) are accepted, not batch handles; meshes whose
+ * padded face count exceeds FVDBM_STATIC_SCRATCH_MAX_FACES are rejected with
+ * FVDBM_EINVAL and a message, before any work is queued.  The first call on
+ * a device looks up the array's device address (once per device and CUDA
+ * context, under a lock: again after the context was re-created, e.g. by
+ * cudaDeviceReset); make that first call before any stream capture.  Every call on a device shares the
  * one array and leaves its last fluxes there (no part of it needs to start
  * at zero: each step writes every face before it reads one); calls whose
  * kernels overlap on the GPU (other streams, other handles, other threads)

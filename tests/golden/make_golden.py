@@ -3,9 +3,9 @@ unmodified ``src/mesher.py``, ``src/containers.py``, ``src/faces.py``,
 ``src/dynamics.py`` and ``src/environment.py`` (from a checkout of
 MADALERAU/FVDBM-JAX) with the numpy stand-in for jax in ``refshim/``.
 
-Usage (needs the reference checkout; only run where it is present):
+Usage (needs a checkout of the reference; its path is required):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout> [--only name,name]
 
 Each case writes ``<name>.npz`` holding the raw mesh, the containers the
 reference's ``Mesher.to_env`` + boundary setters produced, the initial
@@ -295,10 +295,12 @@ def main(ref_path):
 ONLY = set()
 
 if __name__ == "__main__":
-    # make_golden.py [reference path] [--only name,name]: regenerate some cases
+    # make_golden.py <reference checkout> [--only name,name]: regenerate some cases
     args = sys.argv[1:]
     if "--only" in args:
         i = args.index("--only")
         ONLY.update(args[i + 1].split(","))
         del args[i:i + 2]
-    main(args[0] if args else "/root/reference")
+    if len(args) != 1 or not os.path.isdir(os.path.join(args[0], "src")):
+        sys.exit("usage: make_golden.py <path of a MADALERAU/FVDBM-JAX checkout> [--only name,name]")
+    main(args[0])

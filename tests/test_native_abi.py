@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     L = nat.lib()
     for n in declared():
         assert hasattr(L, n), n
-    assert L.fvdbm_abi_version() == 3
+    assert L.fvdbm_abi_version() == 4
 
 
 def _tiny_mesh(**over):

@@ -64,8 +64,8 @@ def test_static_scratch_matches_step(flux):
         new.close()
 
 
-def test_static_scratch_rejects_oversize_and_fused():
-    from fvdbm_jax_gb300 import D2Q9, Environment, Mesher, meshgen
+def test_static_scratch_rejects_oversize_fused_and_batch():
+    from fvdbm_jax_gb300 import D2Q9, Batch, Environment, Mesher, meshgen
     from fvdbm_jax_gb300 import _native as nat
     L = nat.lib()
     m = Mesher().import_meshpy(meshgen.cavity(230))
@@ -76,14 +76,24 @@ def test_static_scratch_rejects_oversize_and_fused():
     big.init()
     fused = Environment(c, f, n, kernel="fused")
     fused.init()
+    # a packed batch steps each case with its own 1/tau and dt and skips
+    # retired cases: the single-mesh staged kernels would not
+    ms = Mesher().import_meshpy(meshgen.cavity(12, seed=1))
+    ms.calc_mesh_properties()
+    cs, fs, ns = ms.to_env(D2Q9(0.6, 0.5 * float(ms.face_lengths.min())), "upwind")
+    batch = Batch([(cs, fs, ns), (cs, fs, ns)])
+    batch.init()
     try:
         assert L.fvdbm_step_static_scratch(big.handle, 1) == -1  # FVDBM_EINVAL
         assert b"at most 131072 padded faces" in L.fvdbm_last_error(big.handle)
         assert L.fvdbm_step_static_scratch(fused.handle, 1) == -1
         assert b"FVDBM_KERNEL_STAGED" in L.fvdbm_last_error(fused.handle)
+        assert L.fvdbm_step_static_scratch(batch.handle, 1) == -1
+        assert b"not a batch" in L.fvdbm_last_error(batch.handle)
         assert L.fvdbm_step_static_scratch(big.handle, -1) == -1
         assert L.fvdbm_step_static_scratch(None, 1) == -1
         nat.check(L.fvdbm_sync(big.handle), big.handle)
     finally:
         big.close()
         fused.close()
+        batch.close()
