@@ -61,7 +61,8 @@ EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", 
            "fvdbm_last_error", "fvdbm_destroy", "fvdbm_abi_version", "fvdbm_const_div_check", "fvdbm_const_div_check_form", "fvdbm_wait_selftest",
            "fvdbm_step_static_scratch", "fvdbm_residual", "fvdbm_run_to_steady",
            "fvdbm_batch_create", "fvdbm_batch_config", "fvdbm_batch_residual", "fvdbm_batch_set_active",
-           "fvdbm_batch_run_to_steady", "fvdbm_set_cells_eq",
+           "fvdbm_batch_run_to_steady", "fvdbm_set_cells_eq", "fvdbm_pack_cells", "fvdbm_unpack_cells",
+           "fvdbm_batch_run_to_steady_time",
            "fvdbm_mp_dense_fwd", "fvdbm_mp_dense_bwd_data", "fvdbm_mp_wgrad_scratch", "fvdbm_mp_dense_bwd_weight",
            "fvdbm_mp_relu_bwd", "fvdbm_mp_spmm", "fvdbm_mp_mse_scratch", "fvdbm_mp_mse", "fvdbm_mp_adam",
            "fvdbm_mp_to_bf16"]
@@ -93,7 +94,11 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_batch_residual.argtypes = [vp, _f64p, _f64p]
     L.fvdbm_batch_set_active.argtypes = [vp, _i32p]
     L.fvdbm_batch_run_to_steady.argtypes = [vp, C.c_double, C.c_int32, _i64p, _i64p, _f64p, _i32p]
+    L.fvdbm_batch_run_to_steady_time.argtypes = [vp, C.c_double, C.c_int32, C.c_double, _i64p, _i64p, _f64p,
+                                                 _i32p]
     L.fvdbm_set_cells_eq.argtypes = [vp, _f32p, _f32p]
+    L.fvdbm_pack_cells.argtypes = [vp, _i32p, C.c_int32, C.c_void_p]
+    L.fvdbm_unpack_cells.argtypes = [vp, _i32p, C.c_int32, C.c_void_p]
     # learned warm start (include/fvdbm_mpnn.h): device pointers as integers
     u64, i32, sz = C.c_uint64, C.c_int32, C.c_size_t
     L.fvdbm_mp_dense_fwd.argtypes = [u64, i32, u64, i32, i32, u64, u64, i32, i32, u64, u64, u64, u64]

@@ -44,19 +44,20 @@ def size_bucket(n_cells: int, n_cases: int, scheme: str) -> str:
 
 
 class Batch:
-    def __init__(self, cases, *, ordering: str = "auto", device: int = 0):
+    def __init__(self, cases, *, ordering: str = "auto", device: int = 0, finite_volume: bool = False):
         self.cases = [from_any(c, f, n) for (c, f, n) in cases]
         if not self.cases:
             raise ValueError("a batch needs at least one case")
         self.ordering, self.device = ordering, device
+        self.finite_volume = finite_volume
         self._h = None
         self.config_used = None
 
     # ------------------------------------------------------------------
     def init(self):
         L = nat.lib()
-        packs = [pack(c, f, n, ordering=self.ordering, kernel="fused", device=self.device)
-                 for (c, f, n) in self.cases]
+        packs = [pack(c, f, n, ordering=self.ordering, kernel="fused", device=self.device,
+                      finite_volume=self.finite_volume) for (c, f, n) in self.cases]
         S = len(packs)
         meshes = (nat.Mesh * S)(*[p[0] for p in packs])
         params = (nat.Params * S)(*[p[1] for p in packs])
@@ -135,17 +136,20 @@ class Batch:
         a = np.ascontiguousarray(np.asarray(active, np.int32).reshape(self.n_cases))
         nat.check(nat.lib().fvdbm_batch_set_active(self._h, nat.iptr(a)), self._h)
 
-    def run_to_steady(self, threshold: float = 1e-6, check_every: int = 100, max_steps=1_000_000):
+    def run_to_steady(self, threshold: float = 1e-6, check_every: int = 100, max_steps=1_000_000,
+                      check_time: float = 0.0):
         """Step until every case's residual is below ``threshold`` (or NaN,
         or its step cap).  Returns per-case (steps, res_u, status) with status
         1 = converged, 0 = step cap, 2 = non-finite, 3 = frozen (residual
         exactly 0 before the threshold: the float32 state stopped changing),
-        4 = stalled (no new residual minimum in 50 checks)."""
+        4 = stalled (no new residual minimum in 50 checks).  ``check_time`` > 0
+        takes each case's residual over a window of at least that much of its
+        own time (``fvdbm_batch_run_to_steady_time``)."""
         S = self.n_cases
         cap = np.ascontiguousarray(np.broadcast_to(np.asarray(max_steps, np.int64), (S,)))
         steps, res, status = np.empty(S, np.int64), np.empty(S, np.float64), np.empty(S, np.int32)
-        nat.check(nat.lib().fvdbm_batch_run_to_steady(
-            self._h, float(threshold), int(check_every), cap.ctypes.data_as(C.POINTER(C.c_int64)),
+        nat.check(nat.lib().fvdbm_batch_run_to_steady_time(
+            self._h, float(threshold), int(check_every), float(check_time), cap.ctypes.data_as(C.POINTER(C.c_int64)),
             steps.ctypes.data_as(C.POINTER(C.c_int64)), res.ctypes.data_as(C.POINTER(C.c_double)),
             nat.iptr(status)), self._h)
         return steps, res, status

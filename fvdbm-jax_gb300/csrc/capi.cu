@@ -45,6 +45,10 @@ struct Handle {
   int* d_active = nullptr;
   int* d_chunk_start = nullptr;  // residual chunks inside the case ranges
   int* d_case_chunk = nullptr;   // first chunk of each case
+  int* d_chunk_case = nullptr;   // case of each chunk
+  int* d_case_take = nullptr;    // [S] cases whose residual a check takes
+  std::vector<long long> case_snap;  // case_steps at each case's snapshot, -1 = none
+  bool usnap_init = false;           // every case's snapshot was written once
   int n_chunks = 0;
   std::vector<float> case_dt_host;
   int* d_blk = nullptr;  // active cell blocks of the batch launch
@@ -74,6 +78,7 @@ struct Handle {
   cudaEvent_t in_ready = nullptr;
   bool in_ok = false;
   int* status_host = nullptr;  // page-locked copy of *status, filled on the stream before a sync
+  int* d_rows = nullptr;       // [N] cell indices of a halo pack/unpack
   std::string err;
 };
 
@@ -653,6 +658,12 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     cs.push_back(hp.N);
     if ((rc = dalloc(h, &h->d_chunk_start, cs.size(), &cs)) != FVDBM_OK) return create_fail(h, rc);
     if ((rc = dalloc(h, &h->d_case_chunk, cc.size(), &cc)) != FVDBM_OK) return create_fail(h, rc);
+    std::vector<int> chc(h->n_chunks);
+    for (int s = 0; s < hp.S; ++s)
+      for (int k = cc[s]; k < cc[s + 1]; ++k) chc[k] = s;
+    if ((rc = dalloc(h, &h->d_chunk_case, chc.size(), &chc)) != FVDBM_OK) return create_fail(h, rc);
+    if ((rc = dalloc<int>(h, &h->d_case_take, size_t(hp.S))) != FVDBM_OK) return create_fail(h, rc);
+    h->case_snap.assign(hp.S, -1);
   }
   if ((rc = dalloc<float>(h, &h->stage, size_t(hp.q) * std::max(hp.N, hp.F))) != FVDBM_OK)
     return create_fail(h, rc);
@@ -744,37 +755,50 @@ int fvdbm_batch_config(void* handle, int32_t block, int32_t prefetch_waves) {
   return update_batch_blocks(h);
 }
 
-int fvdbm_batch_residual(void* handle, double* res_u, double* mass) {
-  if (!handle || !res_u || !mass) return FVDBM_EINVAL;
-  Handle* h = static_cast<Handle*>(handle);
-  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+// Residual and mass of the cases with take[s] != 0 (all when take is null):
+// each over the steps that case took since its own snapshot, which is then
+// renewed; other cases keep their snapshots (res_u and mass untouched).
+static int batch_residual_take(Handle* h, const int32_t* take, double* res_u, double* mass) {
   const HostPlan& hp = h->hp;
   const int S = hp.S;
   CK(cudaSetDevice(h->device));
   int rc;
   if (!h->usnap && (rc = dalloc<float>(h, &h->usnap, size_t(2) * hp.Np)) != FVDBM_OK) return rc;
   if (!h->bred && (rc = dalloc<double>(h, &h->bred, size_t(4) * (h->n_chunks + S))) != FVDBM_OK) return rc;
-  const bool have = h->snap_step >= 0;
+  std::vector<int> tk(S, 1);
+  if (take && h->usnap_init)
+    for (int s = 0; s < S; ++s) tk[s] = take[s] ? 1 : 0;
+  CK(cudaMemcpyAsync(h->d_case_take, tk.data(), S * sizeof(int), cudaMemcpyHostToDevice, h->stream));
   double* out = h->bred + size_t(4) * h->n_chunks;
-  CK(launch_residual(h->dp, h->f[h->cur], h->usnap, h->d_area, have, kResidualChunk, h->d_chunk_start,
-                     h->n_chunks, h->bred, h->d_case_chunk, S, out, h->stream));
+  CK(launch_residual(h->dp, h->f[h->cur], h->usnap, h->d_area, h->usnap_init, kResidualChunk, h->d_chunk_start,
+                     h->n_chunks, h->bred, h->d_case_chunk, S, out, h->stream, h->d_chunk_case, h->d_case_take));
   std::vector<double> tot(size_t(4) * S);
   CK(cudaMemcpyAsync(tot.data(), out, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaStreamSynchronize(h->stream));  // (also: tk is read before it goes out of scope)
   if ((rc = check_status(h)) != FVDBM_OK) return rc;
-  const long long K = h->steps_done - h->snap_step;
   for (int s = 0; s < S; ++s) {
+    if (!tk[s]) continue;
     const double* t = &tot[size_t(4) * s];
+    const long long K = h->case_snap[s] >= 0 ? h->case_steps[s] - h->case_snap[s] : 0;
     mass[s] = t[2];
     if (t[3] > 0.0)
       res_u[s] = std::nan("");
-    else if (!have || K <= 0)
+    else if (!h->usnap_init || h->case_snap[s] < 0 || K <= 0)
       res_u[s] = HUGE_VAL;
     else
       res_u[s] = std::sqrt(t[0]) / (double(K) * double(h->case_dt_host[s]) * std::max(std::sqrt(t[1]), 1e-30));
+    h->case_snap[s] = h->case_steps[s];
   }
+  h->usnap_init = true;
   h->snap_step = h->steps_done;
   return FVDBM_OK;
+}
+
+int fvdbm_batch_residual(void* handle, double* res_u, double* mass) {
+  if (!handle || !res_u || !mass) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+  return batch_residual_take(h, nullptr, res_u, mass);
 }
 
 int fvdbm_batch_set_active(void* handle, const int32_t* active) {
@@ -802,26 +826,32 @@ int fvdbm_batch_set_active(void* handle, const int32_t* active) {
   return FVDBM_OK;
 }
 
-int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_every, const int64_t* max_steps,
-                              int64_t* steps, double* res_u, int32_t* status) {
+int fvdbm_batch_run_to_steady_time(void* handle, double threshold, int32_t check_every, double check_time,
+                                   const int64_t* max_steps, int64_t* steps, double* res_u, int32_t* status) {
   if (!handle || !max_steps || !steps || !res_u || !status) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
   h->in_ok = false;
   if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
   if (check_every <= 0) return fail(h, FVDBM_EINVAL, "check_every <= 0");
+  if (!(check_time >= 0.0)) return fail(h, FVDBM_EINVAL, "check_time must be >= 0");
   const int S = h->hp.S;
-  std::vector<int32_t> act(S), since_best(S, 0);
+  std::vector<int32_t> act(S), since_best(S, 0), take(S, 0);
   std::vector<double> r(S, HUGE_VAL), m(S), best(S, HUGE_VAL);
+  std::vector<int64_t> window(S, check_every);
   for (int s = 0; s < S; ++s) {
     if (max_steps[s] < 0) return fail(h, FVDBM_EINVAL, "max_steps < 0");
     steps[s] = 0;
     res_u[s] = HUGE_VAL;
     status[s] = FVDBM_CASE_CAPPED;
     act[s] = max_steps[s] > 0;
+    // a check covers at least check_time units of the case's own time
+    if (check_time > 0.0)
+      window[s] = std::max<int64_t>(1, int64_t(std::ceil(check_time / double(h->case_dt_host[s]))));
   }
   int rc = fvdbm_batch_set_active(h, act.data());
   if (rc != FVDBM_OK) return rc;
-  if ((rc = fvdbm_batch_residual(h, r.data(), m.data())) != FVDBM_OK) return rc;  // snapshot
+  if ((rc = batch_residual_take(h, nullptr, r.data(), m.data())) != FVDBM_OK) return rc;  // snapshots
+  std::vector<int64_t> since(S, 0);  // steps since the case's snapshot
   for (;;) {
     int64_t n = check_every;
     bool any = false;
@@ -832,11 +862,22 @@ int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_ever
       }
     if (!any) break;
     if ((rc = fvdbm_step(h, int32_t(n))) != FVDBM_OK) return rc;
-    for (int s = 0; s < S; ++s)
-      if (act[s]) steps[s] += n;
-    if ((rc = fvdbm_batch_residual(h, r.data(), m.data())) != FVDBM_OK) return rc;
+    bool check = false;
     for (int s = 0; s < S; ++s) {
+      take[s] = 0;
       if (!act[s]) continue;
+      steps[s] += n;
+      since[s] += n;
+      if (since[s] >= window[s] || steps[s] >= max_steps[s]) {
+        take[s] = 1;
+        check = true;
+      }
+    }
+    if (!check) continue;
+    if ((rc = batch_residual_take(h, take.data(), r.data(), m.data())) != FVDBM_OK) return rc;
+    for (int s = 0; s < S; ++s) {
+      if (!take[s]) continue;
+      since[s] = 0;
       res_u[s] = r[s];
       if (r[s] < best[s]) {
         best[s] = r[s];
@@ -865,6 +906,11 @@ int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_ever
   return FVDBM_OK;
 }
 
+int fvdbm_batch_run_to_steady(void* handle, double threshold, int32_t check_every, const int64_t* max_steps,
+                              int64_t* steps, double* res_u, int32_t* status) {
+  return fvdbm_batch_run_to_steady_time(handle, threshold, check_every, 0.0, max_steps, steps, res_u, status);
+}
+
 int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, const float* node_rho,
                     const float* node_vel) {
   if (!handle) return FVDBM_EINVAL;
@@ -889,6 +935,7 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
       if (!h->active[s])
         CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
     h->snap_step = -1;
+    if (!h->case_snap.empty()) h->case_snap.assign(h->case_snap.size(), -1);
     h->nodes_ready = false;
   }
   if (node_pdf || node_rho || node_vel) {
@@ -899,6 +946,53 @@ int fvdbm_set_state(void* handle, const float* cell_pdf, const float* node_pdf, 
     if (rc != FVDBM_OK) return rc;
   }
   if (read_later) CK(cudaStreamSynchronize(h->stream));  // the caller may reuse its arrays on return
+  return FVDBM_OK;
+}
+
+// Halo rows of a domain decomposition (fvdbm_pack_cells / fvdbm_unpack_cells):
+// checks the cell list and stages it on the device.
+static int stage_rows(Handle* h, const int32_t* cells, int32_t n, const void* buf, const char* who) {
+  const HostPlan& hp = h->hp;
+  if (n < 0 || n > hp.N || (n > 0 && (!cells || !buf)))
+    return fail(h, FVDBM_EINVAL, std::string(who) + ": need 0 <= n <= n_cells, a cell list and a buffer");
+  if (h->batch) return fail(h, FVDBM_EINVAL, std::string(who) + ": not for batch handles");
+  for (int32_t k = 0; k < n; ++k)
+    if (cells[k] < 0 || cells[k] >= hp.N)
+      return fail(h, FVDBM_EINVAL, std::string(who) + ": cell index " + std::to_string(cells[k]) +
+                                       " at position " + std::to_string(k) + " out of range");
+  CK(cudaSetDevice(h->device));
+  if (n == 0) return FVDBM_OK;
+  if (!h->d_rows) {
+    int rc = dalloc<int>(h, &h->d_rows, size_t(hp.N));
+    if (rc != FVDBM_OK) return rc;
+  }
+  // pageable source: the copy has finished reading it when the call returns
+  CK(cudaMemcpyAsync(h->d_rows, cells, size_t(n) * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  return FVDBM_OK;
+}
+
+int fvdbm_pack_cells(void* handle, const int32_t* cells, int32_t n, float* buf) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
+  int rc = stage_rows(h, cells, n, buf, "fvdbm_pack_cells");
+  if (rc != FVDBM_OK || n == 0) return rc;
+  CK(launch_pack_rows(h->f[h->cur], h->d_cell_new, h->d_rows, n, buf, h->stream, h->hp.q));
+  return FVDBM_OK;
+}
+
+int fvdbm_unpack_cells(void* handle, const int32_t* cells, int32_t n, const float* buf) {
+  if (!handle) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  h->in_ok = false;
+  int rc = stage_rows(h, cells, n, buf, "fvdbm_unpack_cells");
+  if (rc != FVDBM_OK || n == 0) return rc;
+  CK(launch_unpack_rows(h->f[h->cur], h->d_cell_new, h->d_rows, n, buf, h->stream, h->hp.q));
+  // an upload of cell pdfs: the node stencils' macros and nodes follow them
+  if (h->fused && h->hp.q == 9) CK(launch_stencil_macros(h->dp, h->f[h->cur], h->stream));
+  h->snap_step = -1;
+    if (!h->case_snap.empty()) h->case_snap.assign(h->case_snap.size(), -1);
+  h->nodes_ready = false;
   return FVDBM_OK;
 }
 
@@ -919,6 +1013,7 @@ int fvdbm_set_cells_eq(void* handle, const float* rho, const float* vel) {
     if (!h->active[s])
       CK(launch_copy_cells(h->f[h->cur], h->f[h->cur ^ 1], hp.case_cell[s], hp.case_cell[s + 1], h->stream));
   h->snap_step = -1;
+    if (!h->case_snap.empty()) h->case_snap.assign(h->case_snap.size(), -1);
   h->nodes_ready = false;
   CK(cudaStreamSynchronize(h->stream));
   return FVDBM_OK;

@@ -290,7 +290,8 @@ cudaError_t launch_macros(const DevPlan& p, const float* f, float* rho, float* v
 int residual_chunks(int N, int chunk);
 cudaError_t launch_residual(const DevPlan& p, const float* f, float* usnap, const float* area,
                             bool have_snap, int chunk, const int* chunk_start, int nchunks,
-                            double* part, const int* seg, int nseg, double* out, cudaStream_t s);
+                            double* part, const int* seg, int nseg, double* out, cudaStream_t s,
+                            const int* chunk_case = nullptr, const int* case_take = nullptr);
 // packed batch: the fused cell kernel with per-case 1/tau, dt and retirement
 // (threads per block 128 or 256; L2 prefetch distance in waves)
 cudaError_t launch_fused_batch(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl,
@@ -312,6 +313,10 @@ cudaError_t launch_gather_cells(const float* src, float* dst_aos, const int* cel
                                 cudaStream_t s, int q = Q);
 // the bounded-wait self-test (fvdbm_wait_selftest)
 cudaError_t launch_wait_selftest(const int* flag, int iters, int* status, cudaStream_t s);
+cudaError_t launch_pack_rows(const float* f, const int* cell_new, const int* idx, int n, float* buf,
+                             cudaStream_t s, int q);
+cudaError_t launch_unpack_rows(float* f, const int* cell_new, const int* idx, int n, const float* buf,
+                               cudaStream_t s, int q);
 // the scatter reading page-locked host memory directly (src 16-byte aligned)
 cudaError_t launch_host_to_cells(const float* src_host, float* dst, const int* cell_new, int N,
                                  cudaStream_t s, int q = Q);

@@ -810,6 +810,26 @@ __global__ void k_cells_to_aos(const float* __restrict__ src, float* __restrict_
   for (int q = 0; q < QQ; ++q) dst[size_t(c) * QQ + q] = b[q * 32];
 }
 
+// Halo exchange of a domain decomposition: rows idx[k] (reference order) of
+// the AoSoA pdf to / from a packed [n][QQ] buffer (coalesced on the buffer).
+template <int QQ>
+__global__ void k_pack_rows(const float* __restrict__ f, const int* __restrict__ cell_new,
+                            const int* __restrict__ idx, int n, float* __restrict__ buf) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * QQ) return;
+  const int k = int(t / QQ), q = int(t % QQ);
+  buf[t] = f[cell_base(cell_new[idx[k]], QQ) + size_t(q) * 32];
+}
+
+template <int QQ>
+__global__ void k_unpack_rows(float* __restrict__ f, const int* __restrict__ cell_new,
+                              const int* __restrict__ idx, int n, const float* __restrict__ buf) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * QQ) return;
+  const int k = int(t / QQ), q = int(t % QQ);
+  f[cell_base(cell_new[idx[k]], QQ) + size_t(q) * 32] = buf[t];
+}
+
 // SoA [rows][Np] device order -> [N][rows] reference order.
 __global__ void k_soa_to_aos(const float* __restrict__ src, float* __restrict__ dst,
                              const int* __restrict__ cell_new, int N, int Np, int rows) {
@@ -1076,6 +1096,28 @@ cudaError_t launch_scatter_cells(const float* src_aos, float* dst, const int* ce
     k_aos_to_cells<13><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
   else
     k_aos_to_cells<Q><<<blocks(N, 256), 256, 0, s>>>(src_aos, dst, cell_new, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_rows(const float* f, const int* cell_new, const int* idx, int n, float* buf,
+                             cudaStream_t s, int q) {
+  if (n <= 0) return cudaSuccess;
+  const int g = blocks((long long)n * q, 256);
+  if (q == 13)
+    k_pack_rows<13><<<g, 256, 0, s>>>(f, cell_new, idx, n, buf);
+  else
+    k_pack_rows<Q><<<g, 256, 0, s>>>(f, cell_new, idx, n, buf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_rows(float* f, const int* cell_new, const int* idx, int n, const float* buf,
+                               cudaStream_t s, int q) {
+  if (n <= 0) return cudaSuccess;
+  const int g = blocks((long long)n * q, 256);
+  if (q == 13)
+    k_unpack_rows<13><<<g, 256, 0, s>>>(f, cell_new, idx, n, buf);
+  else
+    k_unpack_rows<Q><<<g, 256, 0, s>>>(f, cell_new, idx, n, buf);
   return cudaGetLastError();
 }
 

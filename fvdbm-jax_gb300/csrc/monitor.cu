@@ -41,13 +41,20 @@ __device__ __forceinline__ void block_sum4(double v[4]) {
 // Block b covers cells [b*chunk, (b+1)*chunk) (or [chunk_start[b],
 // chunk_start[b+1]) when a table is given) in a fixed per-thread order and
 // writes {sum |du|^2, sum |u_snap|^2, sum rho*A, non-finite cells}.  The
-// snapshot is replaced by the current velocity.
+// snapshot is replaced by the current velocity.  With chunk_case/case_take,
+// a chunk whose case is not taken writes zeros and keeps its snapshot.
 __global__ void __launch_bounds__(RT) k_residual_part(DevPlan p, const float* __restrict__ f,
                                                      float* __restrict__ usnap,
                                                      const float* __restrict__ area, int have_snap,
                                                      int chunk, const int* __restrict__ chunk_start,
+                                                     const int* __restrict__ chunk_case,
+                                                     const int* __restrict__ case_take,
                                                      double* __restrict__ part) {
   double v[4] = {0.0, 0.0, 0.0, 0.0};
+  if (chunk_case && !case_take[chunk_case[blockIdx.x]]) {
+    if (threadIdx.x < 4) part[size_t(blockIdx.x) * 4 + threadIdx.x] = 0.0;
+    return;
+  }
   const int c0 = chunk_start ? chunk_start[blockIdx.x] : blockIdx.x * chunk;
   const int c1 = chunk_start ? chunk_start[blockIdx.x + 1] : min(p.N, c0 + chunk);
   const size_t Np = p.Np;
@@ -95,10 +102,12 @@ int residual_chunks(int N, int chunk) { return N > 0 ? (N + chunk - 1) / chunk :
 
 cudaError_t launch_residual(const DevPlan& p, const float* f, float* usnap, const float* area,
                             bool have_snap, int chunk, const int* chunk_start, int nchunks,
-                            double* part, const int* seg, int nseg, double* out, cudaStream_t s) {
+                            double* part, const int* seg, int nseg, double* out, cudaStream_t s,
+                            const int* chunk_case, const int* case_take) {
   const int nb = chunk_start ? nchunks : residual_chunks(p.N, chunk);
   if (nb > 0)
-    k_residual_part<<<nb, RT, 0, s>>>(p, f, usnap, area, have_snap ? 1 : 0, chunk, chunk_start, part);
+    k_residual_part<<<nb, RT, 0, s>>>(p, f, usnap, area, have_snap ? 1 : 0, chunk, chunk_start, chunk_case,
+                                      case_take, part);
   k_residual_final<<<seg ? nseg : 1, RT, 0, s>>>(part, seg, nb, out);
   return cudaGetLastError();
 }

@@ -150,6 +150,22 @@ int fvdbm_create(const fvdbm_mesh_t *mesh, const fvdbm_params_t *params, void **
 int fvdbm_set_state(void *handle, const float *cell_pdf, const float *node_pdf,
                     const float *node_rho, const float *node_vel);
 
+/* Halo exchange of a domain decomposition (no counterpart in the
+ * reference, which steps one domain).  A rank's handle holds its owned cells
+ * plus a one-ring halo of read-only cells (fvdbm-jax_gb300/partition.py
+ * builds the sub-meshes); after each step it packs the owned rows its
+ * neighbours read, the buffers move to the neighbours (peer copy, NCCL
+ * send/recv, or through the host), and each neighbour unpacks them over its
+ * halo rows.  buf is [n][Q] float32 rows of Cells.pdf for cells[0..n) (this
+ * handle's own, reference-order cell indices), in memory the device
+ * addresses (device memory or page-locked host memory).  Stream-ordered on
+ * fvdbm_stream(handle); cells is read before the call returns.  Unpacking
+ * counts as an upload of cell pdfs: boundary nodes are recomputed before the
+ * next step.  FVDBM_EINVAL for an index outside [0, n_cells) or a batch
+ * handle. */
+int fvdbm_pack_cells(void *handle, const int32_t *cells, int32_t n, float *buf);
+int fvdbm_unpack_cells(void *handle, const int32_t *cells, int32_t n, const float *buf);
+
 /* Cell pdfs set to the equilibrium of given macros, f = feq(rho, u)
  * (src/dynamics.py:70-74, the form Container.__init__ uses for its default
  * state, src/containers.py:24-30): the warm start.  rho [N], vel [N][2]. */
@@ -292,6 +308,20 @@ int fvdbm_batch_set_active(void *handle, const int32_t *active);
 #define FVDBM_CASE_FROZEN 3
 #define FVDBM_CASE_STALLED 4
 #define FVDBM_STALL_CHECKS 50
+
+/* The same with each case's check window in its own time: the cases step
+ * together in chunks of check_every steps, and a case's residual is taken
+ * once it has advanced at least check_time time units (ceil(check_time /
+ * delta_t_s) steps, rounded up to whole chunks) since its last check, or at
+ * its step cap; res_u then measures the change over that window (K is the
+ * case's own step count).  A float32 state keeps rounding-level changes in u
+ * after it has converged; measured over a window of K steps their residual
+ * is about 2e-6 / (K * delta_t), so a window of a few time units keeps that
+ * floor below a 1e-6 threshold for every case whatever its delta_t.
+ * check_time 0 is fvdbm_batch_run_to_steady. */
+int fvdbm_batch_run_to_steady_time(void *handle, double threshold, int32_t check_every, double check_time,
+                                   const int64_t *max_steps, int64_t *steps, double *res_u,
+                                   int32_t *status);
 int fvdbm_batch_run_to_steady(void *handle, double threshold, int32_t check_every,
                               const int64_t *max_steps, int64_t *steps, double *res_u,
                               int32_t *status);
