@@ -4,11 +4,19 @@
 //
 // Weights are bfloat16 (a fp32 master copy lives with the optimiser);
 // activations, accumulations and gradients are float32.  Every reduction has
-// a fixed order (per-block partials combined in block order), so training is
-// bitwise reproducible run to run.  The layers are small (64 hidden units):
-// the work is bound by reading the activations, so the kernels stage
-// activation tiles and the (converted) weights in shared memory and use FP32
-// FMAs.
+// a fixed order (per-block partials combined in block order, the tensor
+// core's own fixed summation inside a tile), so training is bitwise
+// reproducible run to run.
+//
+// The dense layers and their weight gradients run on the tensor cores as
+// warp-level mma.sync m16n8k8 TF32 products with FP32 accumulation.  A bf16
+// weight is exact in TF32 (8 of TF32's 10 mantissa bits).  An FP32 operand x
+// is split into hi = tf32(x) and lo = tf32(x - hi), which together carry 21
+// of its 24 mantissa bits, and its products are formed as hi*w + lo*w (and
+// hi*y + hi*yl + lo*y when both operands are FP32: the weight gradient), the
+// split-precision scheme of Markidis et al., "NVIDIA Tensor Core
+// Programmability, Performance & Precision" (IPDPSW 2018), restated here for
+// TF32.  The result agrees with FP32 FMA accumulation to about 1e-6 relative.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -19,13 +27,219 @@ namespace fvdbm {
 namespace {
 
 constexpr int DT = 256;       // threads per block of the dense kernels
-constexpr int TC = 32;        // cells per tile
-constexpr int GROUPS = DT / TC;  // threads per cell
 constexpr int MAXK = 128;     // input width limit
 constexpr int MAXO = 128;     // output width limit
 constexpr int WG_MAX_ENTRIES = 64 * 128 + 64;  // weight-gradient entries per block (+ bias)
 
-__device__ __forceinline__ float bf16f(uint16_t w) { return __uint_as_float(uint32_t(w) << 16); }
+// TF32 helpers: round to nearest (ties away, cvt.rna) and the hi/lo split.
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - __uint_as_float(hi));
+}
+
+// D += A (16x8, row) * B (8x8, col), TF32 inputs, FP32 accumulators.
+// Fragments (lane = 4*g + t): a0 (g, t), a1 (g+8, t), a2 (g, t+4),
+// a3 (g+8, t+4); b0 (k t, n g), b1 (k t+4, n g); c0 (g, 2t), c1 (g, 2t+1),
+// c2 (g+8, 2t), c3 (g+8, 2t+1).
+__device__ __forceinline__ void mma_tf32(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int TCW = 8;               // warps per block of the tensor-core dense kernels
+constexpr int TCM = 16 * TCW;        // cells per tile (16 rows per warp)
+constexpr int TCO = MAXO;            // padded output width limit (multiple of 8)
+
+// Out[c][o] = sum_k In[c][k] * Wm[k][o] on the tensor cores; same arguments
+// and epilogue as k_dense.  Shared memory: the weights as bf16 bits
+// [Kp][Op + 8] (zero padded) and an activation tile [TCM][Kp + 4] (padded
+// strides keep the fragment loads free of bank conflicts).  Each warp owns
+// 16 cells of the tile and all Op/8 output column blocks.
+template <bool TRANS>
+__global__ void __launch_bounds__(TCW * 32) k_dense_tc(const float* __restrict__ xa, int da,
+                                                       const float* __restrict__ xb, int db, int n,
+                                                       const uint16_t* __restrict__ w,
+                                                       const float* __restrict__ bias, int dout, int relu,
+                                                       const float* __restrict__ residual, float* __restrict__ z,
+                                                       float* __restrict__ ya, int split, int acc_a,
+                                                       float* __restrict__ yb) {
+  extern __shared__ float sm[];
+  const int K = da + db;
+  const int Kp = (K + 7) & ~7, Op = (dout + 7) & ~7;
+  const int ws = Op + 8, xsd = Kp + 4;
+  uint16_t* wm = reinterpret_cast<uint16_t*>(sm);                          // [Kp][ws]
+  float* xs = sm + ((size_t(Kp) * ws + 1) / 2 + 3) / 4 * 4;                 // [TCM][xsd]
+  for (int e = threadIdx.x; e < Kp * ws; e += blockDim.x) {
+    const int k = e / ws, o = e % ws;
+    uint16_t v = 0;
+    if (k < K && o < dout) v = TRANS ? w[size_t(o) * K + k] : w[size_t(k) * dout + o];
+    wm[e] = v;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int ntile = (n + TCM - 1) / TCM;
+  const int NB = Op / 8;
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    __syncthreads();  // weights ready / previous tile consumed
+    const int c0 = tile * TCM;
+    for (int e = threadIdx.x; e < TCM * Kp; e += blockDim.x) {
+      const int cc = e / Kp, k = e % Kp;
+      const int i = c0 + cc;
+      float v = 0.0f;
+      if (i < n && k < K) v = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
+      xs[cc * xsd + k] = v;
+    }
+    __syncthreads();
+    float acc[TCO / 8][4];
+#pragma unroll
+    for (int j = 0; j < TCO / 8; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[j][r] = 0.0f;
+    const float* xr = xs + (warp * 16) * xsd;
+    for (int k0 = 0; k0 < Kp; k0 += 8) {
+      uint32_t ah[4], al[4];
+      split_tf32(xr[g * xsd + k0 + t], ah[0], al[0]);
+      split_tf32(xr[(g + 8) * xsd + k0 + t], ah[1], al[1]);
+      split_tf32(xr[g * xsd + k0 + t + 4], ah[2], al[2]);
+      split_tf32(xr[(g + 8) * xsd + k0 + t + 4], ah[3], al[3]);
+      const uint16_t* w0 = wm + (k0 + t) * ws + g;
+      const uint16_t* w1 = wm + (k0 + t + 4) * ws + g;
+#pragma unroll
+      for (int j = 0; j < TCO / 8; ++j) {
+        if (j < NB) {
+          const uint32_t b0 = uint32_t(w0[8 * j]) << 16, b1 = uint32_t(w1[8 * j]) << 16;
+          mma_tf32(acc[j], al, b0, b1);
+          mma_tf32(acc[j], ah, b0, b1);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < TCO / 8; ++j) {
+      if (j >= NB) break;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int i = c0 + warp * 16 + g + (r >= 2 ? 8 : 0);
+        const int o = 8 * j + 2 * t + (r & 1);
+        if (i >= n || o >= dout) continue;
+        const float a = acc[j][r];
+        if (TRANS) {
+          const float zz = a + (bias ? bias[o] : 0.0f);
+          if (z) z[size_t(i) * dout + o] = zz;
+          float yy = relu ? fmaxf(zz, 0.0f) : zz;
+          if (residual) yy += residual[size_t(i) * dout + o];
+          ya[size_t(i) * dout + o] = yy;
+        } else if (o < split) {
+          float* p = ya + size_t(i) * split + o;
+          *p = acc_a ? *p + a : a;
+        } else {
+          yb[size_t(i) * (dout - split) + (o - split)] = a;
+        }
+      }
+    }
+  }
+}
+
+size_t dense_tc_smem(int K, int dout) {
+  const int Kp = (K + 7) & ~7, Op = (dout + 7) & ~7;
+  const size_t wfl = ((size_t(Kp) * (Op + 8) + 1) / 2 + 3) / 4 * 4;
+  return sizeof(float) * (wfl + size_t(TCM) * (Kp + 4));
+}
+
+// Weight gradient on the tensor cores: per block (a fixed range of `chunk`
+// cells) partial dW[o][k] = sum_c dz[c][o] x[c][k] and db[o] = sum_c dz[c][o]
+// (the bias as a column of ones appended to x).  M = dout (padded to 16s),
+// N = K + 1 (padded to 8s), reduction over the cells in steps of 8; both
+// operands FP32, split hi/lo: hi*hi + hi*lo + lo*hi.  Warp w owns m-tile
+// (w % MT) and the n-blocks w / MT, w / MT + NW, ...
+constexpr int WCT = 64;  // cells per staged slab
+__global__ void __launch_bounds__(TCW * 32) k_dense_wgrad_tc(const float* __restrict__ dz, int n, int dout,
+                                                            const float* __restrict__ xa, int da,
+                                                            const float* __restrict__ xb, int db, int chunk,
+                                                            float* __restrict__ part) {
+  extern __shared__ float sm[];
+  const int K = da + db;
+  const int Mp = (dout + 15) & ~15, Np = (K + 1 + 7) & ~7;
+  const int zsd = Mp + 4, xsd = Np + 8;
+  float* zs = sm;                  // [WCT][zsd]   dz slab, cells x outputs
+  float* xs = sm + WCT * zsd;      // [WCT][xsd]   x slab (+ ones column), cells x inputs
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int MT = Mp / 16, NBk = Np / 8;
+  const int mt = warp % MT, NW = TCW / MT > 0 ? TCW / MT : 1;
+  const bool active = warp < MT * NW;
+  constexpr int MAXJ = (TCO + 8) / 8;  // n-blocks per warp, at most
+  float acc[MAXJ][4];
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[j][r] = 0.0f;
+  const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  for (int s0 = b0; s0 < b1; s0 += WCT) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < WCT * Mp; e += blockDim.x) {
+      const int cc = e / Mp, o = e % Mp, i = s0 + cc;
+      zs[cc * zsd + o] = (i < b1 && o < dout) ? dz[size_t(i) * dout + o] : 0.0f;
+    }
+    for (int e = threadIdx.x; e < WCT * Np; e += blockDim.x) {
+      const int cc = e / Np, k = e % Np, i = s0 + cc;
+      float v = 0.0f;
+      if (i < b1) {
+        if (k < K) v = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
+        else if (k == K) v = 1.0f;
+      }
+      xs[cc * xsd + k] = v;
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int c8 = 0; c8 < WCT; c8 += 8) {
+      // A = dz^T: rows o (m-tile), cols = cells c8..c8+7
+      uint32_t ah[4], al[4];
+      const int o0 = mt * 16;
+      split_tf32(zs[(c8 + t) * zsd + o0 + g], ah[0], al[0]);
+      split_tf32(zs[(c8 + t) * zsd + o0 + g + 8], ah[1], al[1]);
+      split_tf32(zs[(c8 + t + 4) * zsd + o0 + g], ah[2], al[2]);
+      split_tf32(zs[(c8 + t + 4) * zsd + o0 + g + 8], ah[3], al[3]);
+#pragma unroll
+      for (int j = 0; j < MAXJ; ++j) {
+        const int nb = warp / MT + j * NW;
+        if (nb < NBk) {
+          uint32_t bh0, bl0, bh1, bl1;
+          split_tf32(xs[(c8 + t) * xsd + nb * 8 + g], bh0, bl0);
+          split_tf32(xs[(c8 + t + 4) * xsd + nb * 8 + g], bh1, bl1);
+          mma_tf32(acc[j], al, bh0, bh1);
+          mma_tf32(acc[j], ah, bl0, bl1);
+          mma_tf32(acc[j], ah, bh0, bh1);
+        }
+      }
+    }
+  }
+  if (!active) return;
+  const int E = dout * K + dout;
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j) {
+    const int nb = warp / MT + j * NW;
+    if (nb >= NBk) break;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int o = mt * 16 + g + (r >= 2 ? 8 : 0);
+      const int k = nb * 8 + 2 * t + (r & 1);
+      if (o >= dout || k > K) continue;
+      const int e = k < K ? o * K + k : dout * K + o;
+      part[size_t(blockIdx.x) * E + e] = acc[j][r];
+    }
+  }
+}
+
+size_t wgrad_tc_smem(int K, int dout) {
+  const int Mp = (dout + 15) & ~15, Np = (K + 1 + 7) & ~7;
+  return sizeof(float) * size_t(WCT) * ((Mp + 4) + (Np + 8));
+}
 
 static int sm_count() {
   static int n = 0;
@@ -37,121 +251,11 @@ static int sm_count() {
   return n;
 }
 
-// Out[c][o] = sum_k In[c][k] * Wm[k][o] (+ bias[o]), In = [Xa | Xb].  Wm is
-// W^T (forward, W [O][K]) or W itself (backward data, W [K][O]).  Epilogue:
-// z = pre-activation (optional store), y = act(z) (+ residual).
-// Backward-data form: out columns [0, split) go to ya (accumulated when
-// acc_a), the rest to yb.
-template <bool TRANS>
-__global__ void __launch_bounds__(DT) k_dense(const float* __restrict__ xa, int da, const float* __restrict__ xb,
-                                              int db, int n, const uint16_t* __restrict__ w,
-                                              const float* __restrict__ bias, int dout, int relu,
-                                              const float* __restrict__ residual, float* __restrict__ z,
-                                              float* __restrict__ ya, int split, int acc_a,
-                                              float* __restrict__ yb) {
-  extern __shared__ float sm[];
-  const int K = da + db;
-  float* wm = sm;                       // [K][dout]
-  float* xs = sm + K * dout;            // [TC][K + 1]
-  for (int e = threadIdx.x; e < K * dout; e += DT) {
-    const int k = e / dout, o = e % dout;
-    wm[e] = TRANS ? bf16f(w[size_t(o) * K + k]) : bf16f(w[size_t(k) * dout + o]);
-  }
-  const int c = threadIdx.x / GROUPS, g = threadIdx.x % GROUPS;
-  const int ntile = (n + TC - 1) / TC;
-  for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-    __syncthreads();  // weights ready / previous tile consumed
-    const int c0 = t * TC;
-    for (int e = threadIdx.x; e < TC * K; e += DT) {
-      const int cc = e / K, k = e % K;
-      const int i = c0 + cc;
-      float v = 0.0f;
-      if (i < n) v = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
-      xs[cc * (K + 1) + k] = v;
-    }
-    __syncthreads();
-    const int i = c0 + c;
-    float acc[MAXO / GROUPS];
-#pragma unroll
-    for (int j = 0; j < MAXO / GROUPS; ++j) acc[j] = 0.0f;
-    const float* xr = xs + c * (K + 1);
-    for (int k = 0; k < K; ++k) {
-      const float a = xr[k];
-      const float* wr = wm + k * dout;
-#pragma unroll
-      for (int j = 0; j < MAXO / GROUPS; ++j) {
-        const int o = g + GROUPS * j;
-        if (o < dout) acc[j] = fmaf(a, wr[o], acc[j]);
-      }
-    }
-    if (i >= n) continue;
-#pragma unroll
-    for (int j = 0; j < MAXO / GROUPS; ++j) {
-      const int o = g + GROUPS * j;
-      if (o >= dout) break;
-      if (TRANS) {
-        const float zz = acc[j] + (bias ? bias[o] : 0.0f);
-        if (z) z[size_t(i) * dout + o] = zz;
-        float yy = relu ? fmaxf(zz, 0.0f) : zz;
-        if (residual) yy += residual[size_t(i) * dout + o];
-        ya[size_t(i) * dout + o] = yy;
-      } else if (o < split) {
-        float* p = ya + size_t(i) * split + o;
-        *p = acc_a ? *p + acc[j] : acc[j];
-      } else {
-        yb[size_t(i) * (dout - split) + (o - split)] = acc[j];
-      }
-    }
-  }
-}
-
-// Per block (a fixed range of `chunk` cells): partial dW[o][k] = sum dz[c][o]
-// x[c][k] and db[o] = sum dz[c][o], entries strided over the threads.
-__global__ void __launch_bounds__(DT) k_dense_wgrad(const float* __restrict__ dz, int n, int dout,
-                                                    const float* __restrict__ xa, int da,
-                                                    const float* __restrict__ xb, int db, int chunk,
-                                                    float* __restrict__ part) {
-  extern __shared__ float sm[];
-  const int K = da + db;
-  float* zs = sm;                 // [TC][dout]
-  float* xs = sm + TC * dout;     // [TC][K]
-  const int E = dout * K + dout;  // weight entries, then bias entries
-  constexpr int PER = (WG_MAX_ENTRIES + DT - 1) / DT;
-  float acc[PER];
-#pragma unroll
-  for (int j = 0; j < PER; ++j) acc[j] = 0.0f;
-  const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
-  for (int c0 = b0; c0 < b1; c0 += TC) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < TC * dout; e += DT) {
-      const int cc = e / dout, o = e % dout, i = c0 + cc;
-      zs[e] = (i < b1) ? dz[size_t(i) * dout + o] : 0.0f;
-    }
-    for (int e = threadIdx.x; e < TC * K; e += DT) {
-      const int cc = e / K, k = e % K, i = c0 + cc;
-      float v = 0.0f;
-      if (i < b1) v = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
-      xs[e] = v;
-    }
-    __syncthreads();
-    const int nc = min(TC, b1 - c0);
-#pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int e = threadIdx.x + DT * j;
-      if (e >= E) break;
-      const int o = e < dout * K ? e / K : e - dout * K;
-      const int k = e < dout * K ? e % K : -1;
-      float s = acc[j];
-      for (int cc = 0; cc < nc; ++cc) s = fmaf(zs[cc * dout + o], k >= 0 ? xs[cc * K + k] : 1.0f, s);
-      acc[j] = s;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int e = threadIdx.x + DT * j;
-    if (e < E) part[size_t(blockIdx.x) * E + e] = acc[j];
-  }
-}
+// Dense layer semantics (k_dense_tc): Out[c][o] = sum_k In[c][k] * Wm[k][o]
+// (+ bias[o]), In = [Xa | Xb].  Wm is W^T (forward, W [O][K]) or W itself
+// (backward data, W [K][O]).  Epilogue: z = pre-activation (optional store),
+// y = act(z) (+ residual).  Backward-data form: out columns [0, split) go to
+// ya (accumulated when acc_a), the rest to yb.
 
 // Sum of the block partials in block order.
 __global__ void k_sum_parts(const float* __restrict__ part, int nparts, int E, float* __restrict__ dw,
@@ -262,12 +366,12 @@ int fvdbm_mp_dense_fwd(const float* xa, int32_t da, const float* xb, int32_t db,
     return -1;
   if (n == 0) return 0;
   const int K = da + db;
-  const size_t smem = sizeof(float) * (size_t(K) * dout + size_t(TC) * (K + 1));
-  auto kern = k_dense<true>;
+  const size_t smem = dense_tc_smem(K, dout);
+  auto kern = k_dense_tc<true>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -2;
-  const int g = std::min(nblk(n, TC), sm_count() * 4);
-  kern<<<g, DT, smem, static_cast<cudaStream_t>(stream)>>>(xa, da, xb, db, n, w, bias, dout, relu, residual, z,
-                                                           y, 0, 0, nullptr);
+  const int g = std::min(nblk(n, TCM), sm_count() * 2);
+  kern<<<g, TCW * 32, smem, static_cast<cudaStream_t>(stream)>>>(xa, da, xb, db, n, w, bias, dout, relu, residual,
+                                                                 z, y, 0, 0, nullptr);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
@@ -278,12 +382,12 @@ int fvdbm_mp_dense_bwd_data(const float* dz, int32_t n, int32_t dout, const uint
     return -1;
   if (n == 0) return 0;
   const int K = dout, O = da + db;
-  const size_t smem = sizeof(float) * (size_t(K) * O + size_t(TC) * (K + 1));
-  auto kern = k_dense<false>;
+  const size_t smem = dense_tc_smem(K, O);
+  auto kern = k_dense_tc<false>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -2;
-  const int g = std::min(nblk(n, TC), sm_count() * 4);
-  kern<<<g, DT, smem, static_cast<cudaStream_t>(stream)>>>(dz, dout, nullptr, 0, n, w, nullptr, O, 0, nullptr,
-                                                           nullptr, dxa, da, acc_a, dxb);
+  const int g = std::min(nblk(n, TCM), sm_count() * 2);
+  kern<<<g, TCW * 32, smem, static_cast<cudaStream_t>(stream)>>>(dz, dout, nullptr, 0, n, w, nullptr, O, 0, nullptr,
+                                                                 nullptr, dxa, da, acc_a, dxb);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
@@ -304,8 +408,10 @@ int fvdbm_mp_dense_bwd_weight(const float* dz, int32_t n, int32_t dout, const fl
   const int parts = (n + chunk - 1) / chunk;
   const int E = dout * K + dout;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t smem = sizeof(float) * size_t(TC) * (dout + K);
-  k_dense_wgrad<<<parts, DT, smem, s>>>(dz, n, dout, xa, da, xb, db, chunk, scratch);
+  const size_t smem = wgrad_tc_smem(K, dout);
+  if (cudaFuncSetAttribute(k_dense_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+    return -2;
+  k_dense_wgrad_tc<<<parts, TCW * 32, smem, s>>>(dz, n, dout, xa, da, xb, db, chunk, scratch);
   k_sum_parts<<<nblk(E, 256), 256, 0, s>>>(scratch, parts, E, dw, dbias, dout * K);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
