@@ -54,7 +54,7 @@ def parse():
                     help="skip the ~4M-triangle point whose per-step traffic is well above L2")
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--kernel", default="auto",
-                    choices=["auto", "one", "fused", "fused_nodes", "staged", "tile", "tile_split"])
+                    choices=["auto", "one", "fused", "fused_nodes", "persist", "staged", "tile", "tile_split"])
     # --workload batch: time-to-steady of many independent cases, batched vs one at a time
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--threshold", type=float, default=1e-6)
@@ -64,9 +64,13 @@ def parse():
     ap.add_argument("--step-cap", type=int, default=None,
                     help="per-case step cap (default: 20000 for batch, 100000 for warmstart)")
     # --workload warmstart: learned warm start against the uniform start
-    ap.add_argument("--train-cases", type=int, default=256)
+    ap.add_argument("--train-cases", type=int, default=400)
     ap.add_argument("--eval-cases", type=int, default=64)
-    ap.add_argument("--epochs", type=int, default=1500)
+    ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--ws-cells", type=str, default="50000,200000",
+                    help="warmstart: cell-count range of the porous geometries")
+    ap.add_argument("--batch-cells", type=int, default=6_000_000,
+                    help="warmstart: cells per training minibatch")
     return ap.parse_args()
 
 
@@ -413,7 +417,7 @@ def run_gb300(args):
     # kernel does the whole step in one launch.
     F = info["n_faces"]
     K3 = int(np.asarray(c.face_indices).shape[1])
-    if info["kernel"] in (3, 5, 7):
+    if info["kernel"] in (3, 5, 7, 8):
         cell_bytes = info["bytes_per_step"]
     elif info["kernel"] == 4:
         cell_bytes = info["bytes_per_step"] - 36.0 * info["n_bc_nodes"]
@@ -475,7 +479,7 @@ def run_gb300(args):
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                      "l2": "flushed between timed steps (2x L2 written, then read back, on the step's stream)",
                      "kernel": {1: "staged", 2: "fused", 3: "tile", 4: "tile_split", 5: "one",
-                                7: "fused_nodes"}[info["kernel"]],
+                                7: "fused_nodes", 8: "persist"}[info["kernel"]],
                      "launches_per_step": info["launches_per_step"],
                      "ctas_per_sm": info["ctas_per_sm"]})
         line = {
@@ -486,7 +490,7 @@ def run_gb300(args):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": profiled_traffic("cell_kernel"),
                          "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile", 4: "k_tile", 5: "k_step",
-                                    7: "k_fused_nodes"}[info["kernel"]],
+                                    7: "k_fused_nodes", 8: "k_persist"}[info["kernel"]],
                          "bytes_per_launch": cell_bytes, "avg_launch_us": round(cell_avg_s * 1e6, 3),
                          "peak_kind": peak_kind,
                          "step_frac": round(step_achieved / peak, 4),
@@ -593,6 +597,7 @@ def run_batch(args):
             "steps_median_cavity": int(np.median(steps_b[kinds == "cavity"])) if (kinds == "cavity").any() else None,
             "steps_median_porous": int(np.median(steps_b[kinds == "porous"])) if (kinds == "porous").any() else None,
             "res_max_converged": float(res_b[st_b == 1].max()) if (st_b == 1).any() else None,
+            "converged_at_exact_fixed_point": int(np.sum((st_b == 1) & (res_b == 0.0))),
             "n_gpus": ws, "scaling": "strong", "dtype": "f32", "data": "synthetic",
             "autotune": tune,
             "config": {"workload": f"{args.cases} independent cases: {n_cav} lid cavities (2k-60k cells, lid 0.1), "
@@ -607,7 +612,7 @@ def run_batch(args):
 def _ws_case(spec):
     from fvdbm_jax_gb300 import cases as CS
     return CS.porous_square(spec["obstacles"], spec["n_target"], spec["tau"], rho_in=spec["rho_in"],
-                            rho_out=spec["rho_out"], porosity=spec["porosity"], delta_t=spec["dt"],
+                            rho_out=spec["rho_out"], porosity=spec["porosity"], fv_dt=1.0,
                             seed=spec["seed"], mesher=True)
 
 
@@ -624,7 +629,13 @@ def run_warmstart(args):
     squares train the network (on the GPU, by the library's kernels); on
     held-out geometries the solver runs to the residual threshold from the
     uniform start and from f = feq(predicted rho, u), with the stall fallback,
-    both as one Batch with the same loop.  Reports steps and seconds."""
+    both as one Batch with the same loop; and the plain solver runs each case
+    alone from the uniform start.  Reports steps and seconds.
+
+    Regime: the finite-volume scaled update, tau = 0.003 (Re 100 with
+    U = 0.1, L = 1 by nu = c_s^2 tau), dt = min(area / perimeter, tau),
+    inlet density 1.01-1.05, outlet 0.95-0.99; residual windows of
+    ``--check-time`` time units per case."""
     import concurrent.futures as cf
     import multiprocessing as mp
 
@@ -635,27 +646,29 @@ def run_warmstart(args):
     from fvdbm_jax_gb300 import warmstart as WS
 
     rng = np.random.default_rng(2024)
+    lo_cells, hi_cells = (int(v) for v in args.ws_cells.split(","))
 
     def spec(i):
-        return {"obstacles": int(rng.integers(10, 41)), "n_target": int(rng.uniform(4000, 8000)), "tau": 0.65,
-                "rho_in": float(rng.uniform(1.01, 1.05)), "rho_out": float(rng.uniform(0.95, 0.99)),
-                "porosity": float(rng.uniform(0.75, 0.85)), "dt": 1.0, "seed": 50_000 + i}
+        return {"obstacles": int(rng.integers(20, 201)), "n_target": int(rng.uniform(lo_cells, hi_cells)),
+                "tau": 0.003, "rho_in": float(rng.uniform(1.01, 1.05)), "rho_out": float(rng.uniform(0.95, 0.99)),
+                "porosity": float(rng.uniform(0.75, 0.85)), "seed": 50_000 + i}
     specs = [spec(i) for i in range(args.train_cases + args.eval_cases)]
     t0 = time.perf_counter()
     # one pool of host workers, started before the first GPU call, builds the
     # cases and later the per-case network inputs
     ex = cf.ProcessPoolExecutor(min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn"))
-    allc = list(ex.map(_ws_case, specs, chunksize=4))
+    allc = list(ex.map(_ws_case, specs, chunksize=2))
     setup_s = time.perf_counter() - t0
     train, evalc = allc[:args.train_cases], allc[args.train_cases:]
     tspec, espec = specs[:args.train_cases], specs[args.train_cases:]
-    thr, every, cap = args.threshold, args.check_every, args.step_cap or 100_000
+    thr, every, cap = args.threshold, args.check_every, args.step_cap or 1_000_000
+    ct = args.check_time
 
     # training data: the solver's own steady states
     t = time.perf_counter()
-    b = Batch([c[1:4] for c in train])
+    b = Batch([c[1:4] for c in train], finite_volume=True)
     b.init()
-    steps_t, res_t, st_t = b.run_to_steady(thr, every, cap)
+    steps_t, res_t, st_t = b.run_to_steady(thr, every, cap, check_time=ct)
     state = b.state()
     data_s = time.perf_counter() - t
     jobs = []
@@ -664,21 +677,23 @@ def run_warmstart(args):
             continue
         rho, vel = WS.macros(b.case_state(s, state)["pdf"])
         jobs.append((case, sp["rho_in"], sp["rho_out"], rho, vel))
-    samples = list(ex.map(_ws_sample, jobs, chunksize=4))
     b.close()
+    del state
+    samples = list(ex.map(_ws_sample, jobs, chunksize=2))
     t = time.perf_counter()
     net = WS.MPNN(seed=0)
-    hist = net.fit(samples, epochs=args.epochs, lr=3e-3, log_every=max(args.epochs // 10, 1))
+    hist = net.fit(samples, epochs=args.epochs, lr=3e-3, log_every=max(args.epochs // 10, 1),
+                   batch_cells=args.batch_cells)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t
 
     # held-out: uniform start against the predicted start
     def timed(init):
-        bb = Batch([c[1:4] for c in evalc])
+        bb = Batch([c[1:4] for c in evalc], finite_volume=True)
         bb.init()
         bb.sync()
         t1 = time.perf_counter()
-        out = WS.run_cases(bb, thr, every, cap, init=init)
+        out = WS.run_cases(bb, thr, every, cap, init=init, check_time=ct)
         bb.sync()
         el = time.perf_counter() - t1
         fin = bb.state()
@@ -689,22 +704,25 @@ def run_warmstart(args):
     t = time.perf_counter()
     esamples = list(ex.map(_ws_sample, [(case, sp["rho_in"], sp["rho_out"], None, None)
                                         for case, sp in zip(evalc, espec)]))
+    feat_s = time.perf_counter() - t
+    t = time.perf_counter()
     for smp, sp in zip(esamples, espec):
         r, v = WS.untarget(net.predict(smp), sp["rho_in"], sp["rho_out"])
         rho.append(r)
         vel.append(v)
-    infer_s = time.perf_counter() - t
+    infer_s = time.perf_counter() - t + feat_s
     ex.shutdown()
     (sw, stw, restarted), warm_s, fin_w = timed((np.concatenate(rho), np.concatenate(vel)))
     # the plain solver as a user runs it: each case alone from the uniform start
     from fvdbm_jax_gb300 import Environment
     seq_s, seq_steps = 0.0, 0
     for case in evalc:
-        env = Environment(*case[1:4])
+        env = Environment(*case[1:4], finite_volume=True)
         env.init()
         env.sync()
+        w = int(np.ceil(max(1, int(np.ceil(ct / float(case[0].delta_t)))) / every)) * every
         t1 = time.perf_counter()
-        n_s, _ = env.run_to_steady(thr, every, cap)
+        n_s, _ = env.run_to_steady(thr, w, cap)
         env.sync()
         seq_s += time.perf_counter() - t1
         seq_steps += n_s
@@ -714,6 +732,7 @@ def run_warmstart(args):
     pr, pv = np.concatenate(rho), np.concatenate(vel)
     drho = np.concatenate([np.full(c[1].pdf.shape[0], s["rho_in"] - s["rho_out"]) for c, s in zip(evalc, espec)])
     total_s = warm_s + infer_s  # the prediction is part of the warm start's cost
+    ecells = np.array([c[1].pdf.shape[0] for c in evalc])
     line = {"metric": f"time-to-steady @{thr:g} resid, warm vs plain (held-out porous squares)",
             "value": round(total_s, 3), "unit": "s", "higher_is_better": False,
             "warm_solve_s": round(warm_s, 3),
@@ -724,17 +743,22 @@ def run_warmstart(args):
             "steps_plain": int(sp_.sum()), "steps_warm": int(sw.sum()),
             "speedup_steps": round(float(sp_.sum()) / max(float(sw.sum()), 1.0), 2),
             "converged_plain": int(np.sum(stp == 1)), "converged_warm": int(np.sum(stw == 1)),
+            "frozen_plain": int(np.sum(stp == 3)), "frozen_warm": int(np.sum(stw == 3)),
             "restarts": int(restarted.sum()), "inference_s": round(infer_s, 3),
             "pred_rel_err_rho": round(float(np.sqrt(np.mean(((pr - rho_p) / drho) ** 2))), 4),
             "pred_rel_err_u": round(float(np.linalg.norm(pv - vel_p) / np.linalg.norm(vel_p)), 4),
             "train": {"cases": len(samples), "cells": int(sum(s.n for s in samples)), "epochs": args.epochs,
-                      "loss": hist, "train_s": round(train_s, 2), "data_s": round(data_s, 2),
+                      "batch_cells": args.batch_cells, "loss": hist, "train_s": round(train_s, 2),
+                      "data_s": round(data_s, 2), "data_converged": int(np.sum(st_t == 1)),
                       "data_steps_median": int(np.median(steps_t))},
-            "n_gpus": 1, "dtype": "f32 solver; bf16 weights / f32 accumulate network", "data": "synthetic",
-            "config": {"workload": f"porous squares, 10-40 obstacles, porosity 0.75-0.85, 4k-8k cells, "
-                                   f"rho_in 1.01-1.05 / rho_out 0.95-0.99, tau 0.65, dt 1.0, upwind; "
+            "eval_cells": int(ecells.sum()),
+            "n_gpus": 1, "dtype": "f32 solver; bf16 weights / f32 accumulate network (TF32 tensor cores)",
+            "data": "synthetic",
+            "config": {"workload": f"porous squares, 20-200 obstacles, porosity 0.75-0.85, {lo_cells}-{hi_cells} "
+                                   f"cells, rho_in 1.01-1.05 / rho_out 0.95-0.99, tau 0.003 (Re 100), "
+                                   f"finite-volume update, dt = min(area/perimeter, tau), upwind; "
                                    f"{args.train_cases} training + {args.eval_cases} held-out geometries",
-                       "check_every": every, "step_cap": cap, "setup_s": round(setup_s, 1)}}
+                       "check_every": every, "check_time": ct, "step_cap": cap, "setup_s": round(setup_s, 1)}}
     print(json.dumps(line), flush=True)
 
 

@@ -17,7 +17,7 @@ FVDBM_UPWIND, FVDBM_LAX_WENDROFF = 0, 1
 VARIANT_NONE, VARIANT_FACE_SCALE, VARIANT_FACE_Q_SCALE = 0, 1, 2
 ORDER_NONE, ORDER_RCM, ORDER_MORTON = 0, 1, 2
 KERNEL_AUTO, KERNEL_STAGED, KERNEL_FUSED, KERNEL_TILE, KERNEL_TILE_SPLIT, KERNEL_ONE = 0, 1, 2, 3, 4, 5
-KERNEL_BATCH, KERNEL_FUSED_NODES = 6, 7
+KERNEL_BATCH, KERNEL_FUSED_NODES, KERNEL_PERSIST = 6, 7, 8
 
 _i32p = C.POINTER(C.c_int32)
 _f32p = C.POINTER(C.c_float)
@@ -62,10 +62,10 @@ EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", 
            "fvdbm_step_static_scratch", "fvdbm_residual", "fvdbm_run_to_steady",
            "fvdbm_batch_create", "fvdbm_batch_config", "fvdbm_batch_residual", "fvdbm_batch_set_active",
            "fvdbm_batch_run_to_steady", "fvdbm_set_cells_eq", "fvdbm_pack_cells", "fvdbm_unpack_cells",
-           "fvdbm_batch_run_to_steady_time",
+           "fvdbm_batch_run_to_steady_time", "fvdbm_batch_residual_cases",
            "fvdbm_mp_dense_fwd", "fvdbm_mp_dense_bwd_data", "fvdbm_mp_wgrad_scratch", "fvdbm_mp_dense_bwd_weight",
            "fvdbm_mp_relu_bwd", "fvdbm_mp_spmm", "fvdbm_mp_mse_scratch", "fvdbm_mp_mse", "fvdbm_mp_adam",
-           "fvdbm_mp_to_bf16"]
+           "fvdbm_mp_to_bf16", "fvdbm_mp_spmm_chunked"]
 
 
 def lib_path() -> str:
@@ -92,6 +92,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_batch_create.argtypes = [C.POINTER(Mesh), C.POINTER(Params), C.c_int32, C.POINTER(vp)]
     L.fvdbm_batch_config.argtypes = [vp, C.c_int32, C.c_int32]
     L.fvdbm_batch_residual.argtypes = [vp, _f64p, _f64p]
+    L.fvdbm_batch_residual_cases.argtypes = [vp, _i32p, _f64p, _f64p]
     L.fvdbm_batch_set_active.argtypes = [vp, _i32p]
     L.fvdbm_batch_run_to_steady.argtypes = [vp, C.c_double, C.c_int32, _i64p, _i64p, _f64p, _i32p]
     L.fvdbm_batch_run_to_steady_time.argtypes = [vp, C.c_double, C.c_int32, C.c_double, _i64p, _i64p, _f64p,
@@ -108,6 +109,7 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_mp_dense_bwd_weight.argtypes = [u64, i32, i32, u64, i32, u64, i32, u64, u64, u64, sz, u64]
     L.fvdbm_mp_relu_bwd.argtypes = [u64, u64, u64, sz, u64]
     L.fvdbm_mp_spmm.argtypes = [u64, u64, u64, i32, u64, i32, u64, i32, u64]
+    L.fvdbm_mp_spmm_chunked.argtypes = [u64, u64, i32, u64, u64, i32, u64, i32, u64, i32, u64, u64]
     L.fvdbm_mp_mse_scratch.argtypes = [sz]
     L.fvdbm_mp_mse_scratch.restype = sz
     L.fvdbm_mp_mse.argtypes = [u64, u64, u64, sz, C.c_float, u64, u64, sz, u64]

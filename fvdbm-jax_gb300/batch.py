@@ -111,12 +111,20 @@ class Batch:
         nat.check(nat.lib().fvdbm_sync(self._h), self._h)
         return self
 
-    def residual(self):
-        """Per-case (res_u, mass) in double (``fvdbm_batch_residual``)."""
+    def residual(self, take=None):
+        """Per-case (res_u, mass) in double (``fvdbm_batch_residual``); with
+        ``take`` (a mask over the cases) only those cases are measured and
+        re-snapshotted (``fvdbm_batch_residual_cases``), the others read NaN."""
         S = self.n_cases
-        r, m = np.empty(S, np.float64), np.empty(S, np.float64)
-        nat.check(nat.lib().fvdbm_batch_residual(self._h, r.ctypes.data_as(C.POINTER(C.c_double)),
-                                                 m.ctypes.data_as(C.POINTER(C.c_double))), self._h)
+        r, m = np.full(S, np.nan), np.full(S, np.nan)
+        if take is None:
+            nat.check(nat.lib().fvdbm_batch_residual(self._h, r.ctypes.data_as(C.POINTER(C.c_double)),
+                                                     m.ctypes.data_as(C.POINTER(C.c_double))), self._h)
+        else:
+            t = np.ascontiguousarray(np.asarray(take, np.int32).reshape(S))
+            nat.check(nat.lib().fvdbm_batch_residual_cases(self._h, nat.iptr(t),
+                                                           r.ctypes.data_as(C.POINTER(C.c_double)),
+                                                           m.ctypes.data_as(C.POINTER(C.c_double))), self._h)
         return r, m
 
     def set_cells_eq(self, rho, vel):
@@ -140,8 +148,9 @@ class Batch:
                       check_time: float = 0.0):
         """Step until every case's residual is below ``threshold`` (or NaN,
         or its step cap).  Returns per-case (steps, res_u, status) with status
-        1 = converged, 0 = step cap, 2 = non-finite, 3 = frozen (residual
-        exactly 0 before the threshold: the float32 state stopped changing),
+        1 = converged (below the threshold, or an exact float32 fixed point
+        reached from a residual below 100 x threshold), 0 = step cap, 2 =
+        non-finite, 3 = frozen (residual exactly 0 far from convergence),
         4 = stalled (no new residual minimum in 50 checks).  ``check_time`` > 0
         takes each case's residual over a window of at least that much of its
         own time (``fvdbm_batch_run_to_steady_time``)."""

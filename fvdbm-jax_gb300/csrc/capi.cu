@@ -37,6 +37,8 @@ struct Handle {
   bool fused = false;
   bool tile = false;
   bool one = false;  // node and cell blocks in one launch
+  bool persist = false;  // FVDBM_KERNEL_PERSIST: one cooperative launch per fvdbm_step call
+  int* bar = nullptr;    // its grid-barrier counter
   // packed batch of independent cases (fvdbm_batch_create)
   bool batch = false;
   int batch_block = 256, batch_waves = 1;
@@ -246,7 +248,18 @@ int ensure_nodes(Handle* h) {
   return FVDBM_OK;
 }
 
+constexpr int kPersistSteps = 4096;  // steps per cooperative launch, at most
+
 int enqueue_steps(Handle* h, int n) {
+  if (h->persist) {
+    for (int done = 0; done < n;) {
+      const int k = std::min(n - done, kPersistSteps);
+      CK(launch_persist(h->dp, h->f[h->cur], h->f[h->cur ^ 1], k, h->bar, h->stream));
+      if (k & 1) h->cur ^= 1;
+      done += k;
+    }
+    return FVDBM_OK;
+  }
   if (h->fnodes) {
     int rc = ensure_nodes(h);
     if (rc != FVDBM_OK) return rc;
@@ -488,6 +501,12 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     return create_fail(h, FVDBM_EINVAL);
   }
   h->one = one_possible && params->kernel == FVDBM_KERNEL_ONE;
+  if (params->kernel == FVDBM_KERNEL_PERSIST && !(hp.fusable && hp.K == 3 && hp.N > 0 && hp.q == 9 && !segs)) {
+    h->err = "the persistent step needs D2Q9 triangles (3 face slots per cell), every cell face slot "
+             "naming a face of that cell, and no per-q flux scale";
+    return create_fail(h, FVDBM_EINVAL);
+  }
+  h->persist = params->kernel == FVDBM_KERNEL_PERSIST;
   if (hp.q == 13) h->tile = h->one = false;
   if (segs) {
     if (!(hp.fusable && hp.K == 3)) {
@@ -602,6 +621,7 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
     UP(tgh_b, hp.tgh_b);
   }
   if ((rc = dalloc<int>(h, &h->status, 4)) != FVDBM_OK) return create_fail(h, rc);
+  if (h->persist && (rc = dalloc<int>(h, &h->bar, 1)) != FVDBM_OK) return create_fail(h, rc);
   CR(cudaMemsetAsync(h->status, 0, 4 * sizeof(int), h->stream));
   p.status = h->status;
   p.step_ctr = h->status + 1;
@@ -801,6 +821,13 @@ int fvdbm_batch_residual(void* handle, double* res_u, double* mass) {
   return batch_residual_take(h, nullptr, res_u, mass);
 }
 
+int fvdbm_batch_residual_cases(void* handle, const int32_t* take, double* res_u, double* mass) {
+  if (!handle || !take || !res_u || !mass) return FVDBM_EINVAL;
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h->batch) return fail(h, FVDBM_EINVAL, "not a batch handle");
+  return batch_residual_take(h, take, res_u, mass);
+}
+
 int fvdbm_batch_set_active(void* handle, const int32_t* active) {
   if (!handle || !active) return FVDBM_EINVAL;
   Handle* h = static_cast<Handle*>(handle);
@@ -836,7 +863,7 @@ int fvdbm_batch_run_to_steady_time(void* handle, double threshold, int32_t check
   if (!(check_time >= 0.0)) return fail(h, FVDBM_EINVAL, "check_time must be >= 0");
   const int S = h->hp.S;
   std::vector<int32_t> act(S), since_best(S, 0), take(S, 0);
-  std::vector<double> r(S, HUGE_VAL), m(S), best(S, HUGE_VAL);
+  std::vector<double> r(S, HUGE_VAL), m(S), best(S, HUGE_VAL), prev(S, HUGE_VAL);
   std::vector<int64_t> window(S, check_every);
   for (int s = 0; s < S; ++s) {
     if (max_steps[s] < 0) return fail(h, FVDBM_EINVAL, "max_steps < 0");
@@ -878,6 +905,7 @@ int fvdbm_batch_run_to_steady_time(void* handle, double threshold, int32_t check
     for (int s = 0; s < S; ++s) {
       if (!take[s]) continue;
       since[s] = 0;
+      prev[s] = res_u[s];
       res_u[s] = r[s];
       if (r[s] < best[s]) {
         best[s] = r[s];
@@ -889,7 +917,9 @@ int fvdbm_batch_run_to_steady_time(void* handle, double threshold, int32_t check
         status[s] = FVDBM_CASE_NONFINITE;
         act[s] = 0;
       } else if (r[s] == 0.0) {
-        status[s] = FVDBM_CASE_FROZEN;
+        // an exact float32 fixed point: converged when the case was already
+        // within two decades of the threshold, else frozen
+        status[s] = prev[s] < 100.0 * threshold ? FVDBM_CASE_CONVERGED : FVDBM_CASE_FROZEN;
         act[s] = 0;
       } else if (r[s] < threshold) {
         status[s] = FVDBM_CASE_CONVERGED;
@@ -1027,7 +1057,7 @@ int fvdbm_step(void* handle, int32_t n_steps) {
   h->in_ok = false;
   if (n_steps == 1 && h->hp.N > 0) CK(cudaEventRecord(h->in_ready, h->stream));
   int n = n_steps;
-  if (n >= kGraphSteps && h->hp.N > 0) {
+  if (n >= kGraphSteps && h->hp.N > 0 && !h->persist) {
     int rc = ensure_nodes(h);  // outside the capture
     if (rc != FVDBM_OK) return rc;
     while (n >= kGraphSteps) {
@@ -1128,6 +1158,15 @@ int fvdbm_step_phase(void* handle, int32_t phase) {
     h->node_cur ^= 1;
     h->cur ^= 1;
     h->steps_done += 1;
+    return FVDBM_OK;
+  }
+  if (h->persist) {  // one launch per step: phase 1 is empty
+    if (phase != 1 && phase != 2) return fail(h, FVDBM_EINVAL, "phase must be 1 or 2");
+    if (phase == 2) {
+      int rc = enqueue_steps(h, 1);
+      if (rc != FVDBM_OK) return rc;
+      h->steps_done += 1;
+    }
     return FVDBM_OK;
   }
   if (phase == 1) {
@@ -1356,11 +1395,12 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->fnodes ? FVDBM_KERNEL_FUSED_NODES : h->batch ? FVDBM_KERNEL_BATCH : h->one ? FVDBM_KERNEL_ONE
+  info->kernel = h->persist ? FVDBM_KERNEL_PERSIST : h->fnodes ? FVDBM_KERNEL_FUSED_NODES
+               : h->batch ? FVDBM_KERNEL_BATCH : h->one ? FVDBM_KERNEL_ONE
                          : h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
                                    : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);
   const int node_launch = (hp.Mc > 0 && !h->one && !h->fnodes && !(h->tile && h->dp.tile_nodes)) ? 1 : 0;
-  info->launches_per_step = node_launch + (h->one || h->tile || h->batch ? 1 : (h->fused ? 1 : 2));
+  info->launches_per_step = h->persist ? 1 : node_launch + (h->one || h->tile || h->batch ? 1 : (h->fused ? 1 : 2));
   info->padded_cells = hp.Np;
   info->ctas_per_sm = h->tile ? tile_ctas_per_sm(h->dp) : 0;
   info->const_division = h->dp.cdiv_mode;

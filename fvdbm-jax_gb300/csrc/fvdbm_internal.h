@@ -268,6 +268,9 @@ cudaError_t launch_nodes_cp(const DevPlan& p, const float* f, cudaStream_t s, bo
 // fused cell kernel that also computes the next step's boundary nodes (node
 // blocks in the grid wait, bounded, for the stencil cells' blocks)
 cudaError_t launch_fused_nodes(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl);
+// n_steps steps in one cooperative launch; f0 is the current buffer; bar is
+// one device int (zeroed by the launch)
+cudaError_t launch_persist(const DevPlan& p, float* f0, float* f1, int n_steps, int* bar, cudaStream_t s);
 // record the stencil macros of f (after an upload of the cell pdfs)
 cudaError_t launch_stencil_macros(const DevPlan& p, const float* f, cudaStream_t s);
 // the whole step in one launch (node blocks then cell blocks, see kernels.cu)

@@ -62,6 +62,14 @@ __device__ __forceinline__ void load_cell(const float* __restrict__ f, int c, fl
   for (int q = 0; q < Q; ++q) out[q] = __ldg(b + q * 32);
 }
 
+// The same through L2 (ld.global.cg): for pdfs that other blocks wrote
+// earlier in the same launch, which the non-coherent path may hold stale.
+__device__ __forceinline__ void load_cell_cg(const float* f, int c, float out[Q]) {
+  const float* b = f + cell_base(c, Q);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) out[q] = __ldcg(b + q * 32);
+}
+
 // Correctly rounded x/y for a divisor known in advance.  With zr = RN(1/y):
 // q0 = RN(x*zr) is within 1.5 ulp of x/y; one correction
 // q1 = RN(q0 + RN(x - q0*y)*zr) (remainder exact through an FMA) makes it

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(NODE_BLOCK_ENTRIES) k_nodes(DevPlan p, const f
 // nodes).  Padded entries read the last cell's macros from f, or from cprod
 // when LAST_CPROD (the last cell is then a stencil cell).  WAIT: wait for the
 // previous kernel before reading cprod.
-template <bool WAIT, bool LAST_CPROD>
+template <bool WAIT, bool LAST_CPROD, bool F_CG = false>
 __device__ __forceinline__ void node_block_cp(const DevPlan& p, int blk, const float* __restrict__ f,
                                               float* __restrict__ npdf, float* __restrict__ nrho,
                                               float* __restrict__ nvel, float (*prod)[NODE_BLOCK_ENTRIES],
@@ -195,7 +195,10 @@ __device__ __forceinline__ void node_block_cp(const DevPlan& p, int blk, const f
         for (int r = 0; r < 3; ++r) lastm[r] = __ldcg(p.cprod + p.last_slot + r * size_t(p.Sp));
     } else {
       float fc[Q];
-      load_cell(f, p.last_cell, fc);
+      if (F_CG)
+        load_cell_cg(f, p.last_cell, fc);
+      else
+        load_cell(f, p.last_cell, fc);
       float rho, ux, uy;
       macros(fc, rho, ux, uy);
       lastm[0] = rho;
@@ -281,6 +284,8 @@ __device__ __forceinline__ void face_other(const DevPlan& p, const float* __rest
       const float mq = (GHOST_CG ? (__ldcg(pa) + __ldcg(pb)) : (__ldg(pa) + __ldg(pb))) / 2.0f;
       o[q] = mq + (mq - f[q]) * rg;
     }
+  } else if (GHOST_CG) {
+    load_cell_cg(fin, other, o);
   } else {
     load_cell(fin, other, o);
   }
@@ -349,8 +354,8 @@ __device__ __forceinline__ void prefetch_l2(const void* ptr, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
 }
 
-// One cell of the fused update.  GHOST_CG: read node pdfs through L2 (they
-// were written earlier in the same launch).  RECORD: node-stencil cells also
+// One cell of the fused update.  GHOST_CG: read node pdfs, and the cell
+// pdfs, through L2 (for data written earlier in the same launch).  RECORD: node-stencil cells also
 // record the macros of their new pdfs.  inv_tau and dt are the cell's case's.
 template <int SCHEME, int VARIANT, bool FV, bool GHOST_CG, bool RECORD = false>
 __device__ __forceinline__ void fused_cell_f(const DevPlan& p, const float* __restrict__ fin,
@@ -404,7 +409,10 @@ __device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __rest
                                            const float nx[3], const float ny[3], const float Ls[3],
                                            const unsigned* __restrict__ hb) {
   float f[Q];
-  load_cell(fin, i, f);
+  if (GHOST_CG)
+    load_cell_cg(fin, i, f);
+  else
+    load_cell(fin, i, f);
   fused_cell_f<SCHEME, VARIANT, FV, GHOST_CG, RECORD>(p, fin, fout, i, f, code, nx, ny, Ls, hb, p.inv_tau, p.dt);
 }
 
@@ -510,6 +518,101 @@ __global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __r
       atomicAdd(&ctr[0], 1);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent multi-step kernel (cooperative launch: every block resident).
+// Step s is the two-launch family's step: the boundary nodes from the
+// recorded stencil macros (cprod), the node kernel's blocks, then the fused cell
+// update of every cell from buffer f[s & 1] into f[(s + 1) & 1], which
+// records cprod for the next step.  A grid barrier separates the phases, so
+// each step costs two barriers instead of two launches.  The barrier is a
+// monotonic arrival counter (zeroed by the host before the launch) with a
+// bounded wait; a wait that runs out sets the status word and every block
+// leaves at its next barrier.
+
+// Grid barrier number k (k = 1, 2, ...): arrive, then wait (thread 0,
+// bounded) until every block has arrived k times.  Returns false, with the
+// status word set, when the wait ran out or another block already gave up.
+__device__ __forceinline__ bool grid_barrier(const DevPlan& p, int* bar, int k, int* s_ok) {
+  __threadfence();  // this thread's writes before the arrival
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1);
+    // a tight spin (no sleep between polls: a barrier lasts about a
+    // microsecond), bounded to 2^24 polls
+    const int target = k * int(gridDim.x);
+    bool ok = false;
+    for (int it = 0; it < (1 << 24); ++it)
+      if (ld_acquire_gpu(bar) >= target) {
+        ok = true;
+        break;
+      }
+    if (!ok) atomicExch(p.status, STATUS_WAIT_TIMEOUT);
+    *s_ok = ok && ld_acquire_gpu(p.status) == 0;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+template <int SCHEME, int VARIANT, bool FV>
+__global__ void __launch_bounds__(256) k_persist(DevPlan p, float* f0, float* f1, int n_steps, int* bar) {
+  __shared__ int s_ok;
+  __shared__ float prod[12][NODE_BLOCK_ENTRIES];
+  __shared__ float lastm[3];
+  const int ncb = (p.N + 255) / 256;
+  int k = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    const float* fin = (s & 1) ? f1 : f0;
+    float* fout = (s & 1) ? f0 : f1;
+    // boundary nodes of step s from the macros of fin (cprod): the node
+    // kernel's entry-parallel blocks, spread over the grid
+    for (int nb = blockIdx.x; nb < p.NB; nb += gridDim.x) {
+      node_block_cp<false, false, true>(p, nb, fin, p.node_pdf, p.node_rho, p.node_vel, prod, lastm);
+      __syncthreads();  // prod is reused by the block's next node block
+    }
+    if (!grid_barrier(p, bar, ++k, &s_ok)) return;
+    // cells of step s
+    for (int cb = blockIdx.x; cb < ncb; cb += gridDim.x) {
+      const int i = cb * 256 + threadIdx.x;
+      const unsigned* hb;
+      int code[3];
+      float nx[3], ny[3], Ls[3];
+      load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
+      if (i < p.N) fused_cell<SCHEME, VARIANT, FV, true, 1>(p, fin, fout, i, code, nx, ny, Ls, hb);
+    }
+    if (!grid_barrier(p, bar, ++k, &s_ok)) return;
+  }
+}
+
+template <int S, int V>
+static cudaError_t persist_dispatch(const DevPlan& p, float* f0, float* f1, int n_steps, int* bar,
+                                    cudaStream_t s) {
+  void (*kern)(DevPlan, float*, float*, int, int*) = p.fv ? k_persist<S, V, true> : k_persist<S, V, false>;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int ncb = (p.N + 255) / 256;
+  const int grid = std::max(1, std::min(std::max(ncb, p.NB), per_sm * sms));
+  e = cudaMemsetAsync(bar, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  DevPlan pp = p;
+  void* args[] = {&pp, &f0, &f1, &n_steps, &bar};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid), dim3(256), args, 0, s);
+}
+
+cudaError_t launch_persist(const DevPlan& p, float* f0, float* f1, int n_steps, int* bar, cudaStream_t s) {
+  if (p.N == 0 || n_steps <= 0) return cudaSuccess;
+  if (p.K != 3) return cudaErrorInvalidValue;
+  if (p.scheme == 0 && p.variant == 0) return persist_dispatch<0, 0>(p, f0, f1, n_steps, bar, s);
+  if (p.scheme == 1 && p.variant == 0) return persist_dispatch<1, 0>(p, f0, f1, n_steps, bar, s);
+  if (p.scheme == 0 && p.variant == 1) return persist_dispatch<0, 1>(p, f0, f1, n_steps, bar, s);
+  if (p.scheme == 1 && p.variant == 1) return persist_dispatch<1, 1>(p, f0, f1, n_steps, bar, s);
+  return cudaErrorInvalidValue;
 }
 
 // Packed batch of independent cases: the same cell update with the cell's

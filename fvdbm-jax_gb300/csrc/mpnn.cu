@@ -58,11 +58,51 @@ constexpr int TCW = 8;               // warps per block of the tensor-core dense
 constexpr int TCM = 16 * TCW;        // cells per tile (16 rows per warp)
 constexpr int TCO = MAXO;            // padded output width limit (multiple of 8)
 
+// Asynchronous 16-byte global -> shared copies (cp.async.cg: through L2).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t d = uint32_t(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Rows [c0, c0 + TCM) of In = [Xa | Xb] into a tile [TCM][xsd]: 16-byte
+// asynchronous copies when both parts' rows are 16-byte aligned (da, db
+// multiples of 4 and aligned bases), else plain loads.  Rows past n are not
+// written (their outputs are never stored); the pad columns [K, Kp) are
+// zeroed once by the caller.
+__device__ __forceinline__ bool rows_vec4(const float* xa, int da, const float* xb, int db) {
+  return (da % 4 == 0) && (db % 4 == 0) && ((reinterpret_cast<uintptr_t>(xa) & 15) == 0) &&
+         (db == 0 || (reinterpret_cast<uintptr_t>(xb) & 15) == 0);
+}
+__device__ __forceinline__ void load_rows(float* xs, int xsd, const float* __restrict__ xa, int da,
+                                          const float* __restrict__ xb, int db, int c0, int rows, int n,
+                                          bool vec) {
+  const int K = da + db;
+  if (vec) {
+    const int K4 = K / 4;
+    for (int e = threadIdx.x; e < rows * K4; e += blockDim.x) {
+      const int cc = e / K4, k = (e % K4) * 4, i = c0 + cc;
+      if (i >= n) continue;
+      const float* src = k < da ? xa + size_t(i) * da + k : xb + size_t(i) * db + (k - da);
+      cp_async16(xs + cc * xsd + k, src);
+    }
+  } else {
+    for (int e = threadIdx.x; e < rows * K; e += blockDim.x) {
+      const int cc = e / K, k = e % K, i = c0 + cc;
+      if (i >= n) continue;
+      xs[cc * xsd + k] = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
+    }
+  }
+}
+
 // Out[c][o] = sum_k In[c][k] * Wm[k][o] on the tensor cores; same arguments
-// and epilogue as k_dense.  Shared memory: the weights as bf16 bits
-// [Kp][Op + 8] (zero padded) and an activation tile [TCM][Kp + 4] (padded
-// strides keep the fragment loads free of bank conflicts).  Each warp owns
-// 16 cells of the tile and all Op/8 output column blocks.
+// and epilogue as the dense layer above.  Shared memory: the weights as bf16
+// bits [Kp][Op + 8] (zero padded) and two activation tiles [TCM][Kp + 4]
+// (padded strides keep the fragment loads free of bank conflicts): the next
+// tile streams in by cp.async while the warps multiply the current one.
+// Each warp owns 16 cells of a tile and all Op/8 output column blocks.
 template <bool TRANS>
 __global__ void __launch_bounds__(TCW * 32) k_dense_tc(const float* __restrict__ xa, int da,
                                                        const float* __restrict__ xb, int db, int n,
@@ -76,27 +116,35 @@ __global__ void __launch_bounds__(TCW * 32) k_dense_tc(const float* __restrict__
   const int Kp = (K + 7) & ~7, Op = (dout + 7) & ~7;
   const int ws = Op + 8, xsd = Kp + 4;
   uint16_t* wm = reinterpret_cast<uint16_t*>(sm);                          // [Kp][ws]
-  float* xs = sm + ((size_t(Kp) * ws + 1) / 2 + 3) / 4 * 4;                 // [TCM][xsd]
+  float* xbuf = sm + ((size_t(Kp) * ws + 1) / 2 + 3) / 4 * 4;               // [2][TCM][xsd]
+  const size_t tile_floats = size_t(TCM) * xsd;
+  const bool vec = rows_vec4(xa, da, xb, db);
+  const int ntile = (n + TCM - 1) / TCM;
+  int tile = blockIdx.x;
+  // first tile in flight while the weights are staged
+  if (tile < ntile) load_rows(xbuf, xsd, xa, da, xb, db, tile * TCM, TCM, n, vec);
+  cp_async_commit();
   for (int e = threadIdx.x; e < Kp * ws; e += blockDim.x) {
     const int k = e / ws, o = e % ws;
     uint16_t v = 0;
     if (k < K && o < dout) v = TRANS ? w[size_t(o) * K + k] : w[size_t(k) * dout + o];
     wm[e] = v;
   }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int ntile = (n + TCM - 1) / TCM;
-  const int NB = Op / 8;
-  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-    __syncthreads();  // weights ready / previous tile consumed
-    const int c0 = tile * TCM;
-    for (int e = threadIdx.x; e < TCM * Kp; e += blockDim.x) {
-      const int cc = e / Kp, k = e % Kp;
-      const int i = c0 + cc;
-      float v = 0.0f;
-      if (i < n && k < K) v = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
-      xs[cc * xsd + k] = v;
+  if (Kp > K)  // pad columns of both tiles: zero, never copied over
+    for (int e = threadIdx.x; e < 2 * TCM * (Kp - K); e += blockDim.x) {
+      const int r = e / (Kp - K), k = K + e % (Kp - K);
+      xbuf[size_t(r) * xsd + k] = 0.0f;
     }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int NB = Op / 8;
+  for (int it = 0; tile < ntile; tile += gridDim.x, ++it) {
+    float* xs = xbuf + (it & 1) * tile_floats;
+    const int next = tile + int(gridDim.x);
+    if (next < ntile) load_rows(xbuf + ((it + 1) & 1) * tile_floats, xsd, xa, da, xb, db, next * TCM, TCM, n, vec);
+    cp_async_commit();
+    cp_async_wait<1>();  // this tile's copies have landed (the next one's may still fly)
     __syncthreads();
+    const int c0 = tile * TCM;
     float acc[TCO / 8][4];
 #pragma unroll
     for (int j = 0; j < TCO / 8; ++j)
@@ -143,13 +191,15 @@ __global__ void __launch_bounds__(TCW * 32) k_dense_tc(const float* __restrict__
         }
       }
     }
+    __syncthreads();  // the tile is consumed before the buffer is refilled
   }
+  cp_async_wait<0>();
 }
 
 size_t dense_tc_smem(int K, int dout) {
   const int Kp = (K + 7) & ~7, Op = (dout + 7) & ~7;
   const size_t wfl = ((size_t(Kp) * (Op + 8) + 1) / 2 + 3) / 4 * 4;
-  return sizeof(float) * (wfl + size_t(TCM) * (Kp + 4));
+  return sizeof(float) * (wfl + 2 * size_t(TCM) * (Kp + 4));
 }
 
 // Weight gradient on the tensor cores: per block (a fixed range of `chunk`
@@ -167,8 +217,18 @@ __global__ void __launch_bounds__(TCW * 32) k_dense_wgrad_tc(const float* __rest
   const int K = da + db;
   const int Mp = (dout + 15) & ~15, Np = (K + 1 + 7) & ~7;
   const int zsd = Mp + 4, xsd = Np + 8;
-  float* zs = sm;                  // [WCT][zsd]   dz slab, cells x outputs
-  float* xs = sm + WCT * zsd;      // [WCT][xsd]   x slab (+ ones column), cells x inputs
+  const size_t slab = size_t(WCT) * (zsd + xsd);  // one buffer: dz slab, then x slab
+  // two buffers [zs | xs]: cells x outputs, cells x inputs (+ ones column)
+  for (int e = threadIdx.x; e < int(2 * slab); e += blockDim.x) {
+    const int bsel = e / int(slab), r = e % int(slab);  // buffer, offset in it
+    float v = 0.0f;
+    if (r >= WCT * zsd && (r - WCT * zsd) % xsd == K) v = 1.0f;  // the bias column of ones
+    (void)bsel;
+    sm[e] = v;
+  }
+  __syncthreads();  // initialised before any copy lands on top of it
+  const bool zvec = (dout % 4 == 0) && ((reinterpret_cast<uintptr_t>(dz) & 15) == 0);
+  const bool xvec = rows_vec4(xa, da, xb, db);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int MT = Mp / 16, NBk = Np / 8;
   const int mt = warp % MT, NW = TCW / MT > 0 ? TCW / MT : 1;
@@ -180,45 +240,66 @@ __global__ void __launch_bounds__(TCW * 32) k_dense_wgrad_tc(const float* __rest
 #pragma unroll
     for (int r = 0; r < 4; ++r) acc[j][r] = 0.0f;
   const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
-  for (int s0 = b0; s0 < b1; s0 += WCT) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < WCT * Mp; e += blockDim.x) {
-      const int cc = e / Mp, o = e % Mp, i = s0 + cc;
-      zs[cc * zsd + o] = (i < b1 && o < dout) ? dz[size_t(i) * dout + o] : 0.0f;
-    }
-    for (int e = threadIdx.x; e < WCT * Np; e += blockDim.x) {
-      const int cc = e / Np, k = e % Np, i = s0 + cc;
-      float v = 0.0f;
-      if (i < b1) {
-        if (k < K) v = k < da ? xa[size_t(i) * da + k] : xb[size_t(i) * db + (k - da)];
-        else if (k == K) v = 1.0f;
+  // one slab of cells [s0, s0 + WCT) into buffer bsel; rows past b1 of the
+  // dz slab are zeroed (they are summed over), x rows keep finite old values
+  auto stage = [&](int s0, int bsel) {
+    float* zs = sm + bsel * slab;
+    float* xs = zs + WCT * zsd;
+    const int rows = min(WCT, b1 - s0);
+    if (zvec) {
+      const int O4 = dout / 4;
+      for (int e = threadIdx.x; e < rows * O4; e += blockDim.x) {
+        const int cc = e / O4, o = (e % O4) * 4;
+        cp_async16(zs + cc * zsd + o, dz + size_t(s0 + cc) * dout + o);
       }
-      xs[cc * xsd + k] = v;
+    } else {
+      for (int e = threadIdx.x; e < rows * dout; e += blockDim.x) {
+        const int cc = e / dout, o = e % dout;
+        zs[cc * zsd + o] = dz[size_t(s0 + cc) * dout + o];
+      }
     }
+    for (int e = threadIdx.x; e < (WCT - rows) * dout; e += blockDim.x) {
+      const int cc = rows + e / dout, o = e % dout;
+      zs[cc * zsd + o] = 0.0f;
+    }
+    load_rows(xs, xsd, xa, da, xb, db, s0, rows, b1, xvec);
+  };
+  int it = 0;
+  if (b0 < b1) stage(b0, 0);
+  cp_async_commit();
+  for (int s0 = b0; s0 < b1; s0 += WCT, ++it) {
+    if (s0 + WCT < b1) stage(s0 + WCT, (it + 1) & 1);
+    cp_async_commit();
+    cp_async_wait<1>();
     __syncthreads();
-    if (!active) continue;
-    for (int c8 = 0; c8 < WCT; c8 += 8) {
-      // A = dz^T: rows o (m-tile), cols = cells c8..c8+7
-      uint32_t ah[4], al[4];
-      const int o0 = mt * 16;
-      split_tf32(zs[(c8 + t) * zsd + o0 + g], ah[0], al[0]);
-      split_tf32(zs[(c8 + t) * zsd + o0 + g + 8], ah[1], al[1]);
-      split_tf32(zs[(c8 + t + 4) * zsd + o0 + g], ah[2], al[2]);
-      split_tf32(zs[(c8 + t + 4) * zsd + o0 + g + 8], ah[3], al[3]);
+    const float* zs = sm + (it & 1) * slab;
+    const float* xs = zs + WCT * zsd;
+    if (active) {
+      for (int c8 = 0; c8 < WCT; c8 += 8) {
+        // A = dz^T: rows o (m-tile), cols = cells c8..c8+7
+        uint32_t ah[4], al[4];
+        const int o0 = mt * 16;
+        split_tf32(zs[(c8 + t) * zsd + o0 + g], ah[0], al[0]);
+        split_tf32(zs[(c8 + t) * zsd + o0 + g + 8], ah[1], al[1]);
+        split_tf32(zs[(c8 + t + 4) * zsd + o0 + g], ah[2], al[2]);
+        split_tf32(zs[(c8 + t + 4) * zsd + o0 + g + 8], ah[3], al[3]);
 #pragma unroll
-      for (int j = 0; j < MAXJ; ++j) {
-        const int nb = warp / MT + j * NW;
-        if (nb < NBk) {
-          uint32_t bh0, bl0, bh1, bl1;
-          split_tf32(xs[(c8 + t) * xsd + nb * 8 + g], bh0, bl0);
-          split_tf32(xs[(c8 + t + 4) * xsd + nb * 8 + g], bh1, bl1);
-          mma_tf32(acc[j], al, bh0, bh1);
-          mma_tf32(acc[j], ah, bl0, bl1);
-          mma_tf32(acc[j], ah, bh0, bh1);
+        for (int j = 0; j < MAXJ; ++j) {
+          const int nb = warp / MT + j * NW;
+          if (nb < NBk) {
+            uint32_t bh0, bl0, bh1, bl1;
+            split_tf32(xs[(c8 + t) * xsd + nb * 8 + g], bh0, bl0);
+            split_tf32(xs[(c8 + t + 4) * xsd + nb * 8 + g], bh1, bl1);
+            mma_tf32(acc[j], al, bh0, bh1);
+            mma_tf32(acc[j], ah, bl0, bl1);
+            mma_tf32(acc[j], ah, bh0, bh1);
+          }
         }
       }
     }
+    __syncthreads();  // the slab is consumed before its buffer is refilled
   }
+  cp_async_wait<0>();
   if (!active) return;
   const int E = dout * K + dout;
 #pragma unroll
@@ -238,7 +319,7 @@ __global__ void __launch_bounds__(TCW * 32) k_dense_wgrad_tc(const float* __rest
 
 size_t wgrad_tc_smem(int K, int dout) {
   const int Mp = (dout + 15) & ~15, Np = (K + 1 + 7) & ~7;
-  return sizeof(float) * size_t(WCT) * ((Mp + 4) + (Np + 8));
+  return 2 * sizeof(float) * size_t(WCT) * ((Mp + 4) + (Np + 8));
 }
 
 static int sm_count() {
@@ -285,6 +366,31 @@ __global__ void k_spmm(const int* __restrict__ row_ptr, const int* __restrict__ 
   if (i >= n) return;
   float s = 0.0f;
   for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) s = fmaf(wt[e], h[size_t(col[e]) * d + f], s);
+  float* o = out + size_t(i) * d + f;
+  *o = accumulate ? *o + s : s;
+}
+
+// Long rows in chunks: pass 1 folds each chunk's entries (at most a few
+// dozen, in order) per feature into partial[chunk][f]; pass 2 folds a row's
+// chunk partials in chunk order.  Fixed order throughout: reproducible.
+__global__ void k_spmm_chunks(const int* __restrict__ chunk_start, const int* __restrict__ col,
+                              const float* __restrict__ wt, int nchunks, const float* __restrict__ h, int d,
+                              float* __restrict__ partial) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int c = int(t / d), f = int(t % d);
+  if (c >= nchunks) return;
+  float s = 0.0f;
+  for (int e = chunk_start[c]; e < chunk_start[c + 1]; ++e) s = fmaf(wt[e], h[size_t(col[e]) * d + f], s);
+  partial[size_t(c) * d + f] = s;
+}
+
+__global__ void k_spmm_rows(const int* __restrict__ chunk_ptr, int n, const float* __restrict__ partial, int d,
+                            float* __restrict__ out, int accumulate) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int i = int(t / d), f = int(t % d);
+  if (i >= n) return;
+  float s = 0.0f;
+  for (int c = chunk_ptr[i]; c < chunk_ptr[i + 1]; ++c) s += partial[size_t(c) * d + f];
   float* o = out + size_t(i) * d + f;
   *o = accumulate ? *o + s : s;
 }
@@ -392,7 +498,7 @@ int fvdbm_mp_dense_bwd_data(const float* dz, int32_t n, int32_t dout, const uint
 }
 
 size_t fvdbm_mp_wgrad_scratch(int32_t n, int32_t dout, int32_t din) {
-  const int chunk = 4096;
+  const int chunk = 1024;  // cells per block of the weight gradient
   const size_t parts = size_t((n + chunk - 1) / chunk);
   return sizeof(float) * std::max<size_t>(parts, 1) * (size_t(dout) * din + dout);
 }
@@ -404,7 +510,7 @@ int fvdbm_mp_dense_bwd_weight(const float* dz, int32_t n, int32_t dout, const fl
   if (n <= 0 || dout <= 0 || dout * K + dout > WG_MAX_ENTRIES || da <= 0 || db < 0 || K > MAXK || !dz || !xa ||
       (db > 0 && !xb) || !dw || !scratch || scratch_bytes < fvdbm_mp_wgrad_scratch(n, dout, K))
     return -1;
-  const int chunk = 4096;
+  const int chunk = 1024;  // cells per block of the weight gradient
   const int parts = (n + chunk - 1) / chunk;
   const int E = dout * K + dout;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -429,6 +535,20 @@ int fvdbm_mp_spmm(const int32_t* row_ptr, const int32_t* col, const float* wt, i
   if (n == 0) return 0;
   k_spmm<<<nblk(size_t(n) * d, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(row_ptr, col, wt, n, h, d, out,
                                                                                  accumulate);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int fvdbm_mp_spmm_chunked(const int32_t* chunk_start, const int32_t* chunk_ptr, int32_t nchunks, const int32_t* col,
+                          const float* wt, int32_t n, const float* h, int32_t d, float* out, int32_t accumulate,
+                          float* partial, void* stream) {
+  if (n < 0 || nchunks < 0 || d <= 0 || !chunk_start || !chunk_ptr || !col || !wt || !h || !out ||
+      (nchunks > 0 && !partial))
+    return -1;
+  if (n == 0) return 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (nchunks > 0)
+    k_spmm_chunks<<<nblk(size_t(nchunks) * d, 256), 256, 0, s>>>(chunk_start, col, wt, nchunks, h, d, partial);
+  k_spmm_rows<<<nblk(size_t(n) * d, 256), 256, 0, s>>>(chunk_ptr, n, partial, d, out, accumulate);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 

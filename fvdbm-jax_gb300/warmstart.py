@@ -39,14 +39,34 @@ SCALES = ("mesh", "c16", "c4", "c1")
 
 # ----------------------------------------------------------------------------
 # graph and features
+SPMM_CHUNK = 64  # entries per chunk of a long row
+
+
+def _chunks(indptr):
+    """Chunks of at most SPMM_CHUNK entries inside each CSR row: entry
+    offsets [nchunks+1] and each row's first chunk [rows+1]."""
+    lens = np.diff(indptr).astype(np.int64)
+    per = (lens + SPMM_CHUNK - 1) // SPMM_CHUNK
+    cptr = np.concatenate([[0], np.cumsum(per)]).astype(np.int32)
+    row = np.repeat(np.arange(lens.size), per)
+    k = np.arange(int(cptr[-1])) - np.repeat(cptr[:-1].astype(np.int64), per)
+    start = (indptr[:-1].astype(np.int64)[row] + k * SPMM_CHUNK)
+    return np.concatenate([start, [int(indptr[-1])]]).astype(np.int32), cptr
+
+
 def _stage(S):
     """One sparse stage of a layer's aggregation: the CSR of S and of S^T
-    (row_ptr, col, wt), each row's entries in ascending column order."""
+    (row_ptr, col, wt, chunk_start, chunk_ptr), each row's entries in
+    ascending column order, cut into chunks for the long rows."""
     S = S.tocsr().astype(np.float32)
     S.sort_indices()
     St = S.T.tocsr()
     St.sort_indices()
-    pack = lambda M: (M.indptr.astype(np.int32), M.indices.astype(np.int32), M.data.astype(np.float32))
+
+    def pack(M):
+        ip = M.indptr.astype(np.int32)
+        cs, cp = _chunks(ip)
+        return (ip, M.indices.astype(np.int32), M.data.astype(np.float32), cs, cp)
     return {"rows": S.shape[0], "cols": S.shape[1], "M": pack(S), "Mt": pack(St)}
 
 
@@ -206,15 +226,22 @@ class Sample:
 
 
 def _cat_csr(mats, rows, cols):
-    """Block-diagonal union of CSR matrices (row/column sizes per block)."""
+    """Block-diagonal union of CSR matrices (row/column sizes per block),
+    with their chunk tables."""
     ptr, col, wt, off_e, off_c = [np.zeros(1, np.int32)], [], [], 0, 0
-    for (p, c, w), nc in zip(mats, cols):
+    cst, cpt, off_k = [], [np.zeros(1, np.int32)], 0
+    for (p, c, w, cs, cp), nc in zip(mats, cols):
         ptr.append(p[1:] + off_e)
         col.append(c + off_c)
         wt.append(w)
+        cst.append(cs[:-1].astype(np.int64) + off_e)
+        cpt.append(cp[1:].astype(np.int64) + off_k)
         off_e += int(p[-1])
         off_c += nc
-    return np.concatenate(ptr).astype(np.int32), np.concatenate(col).astype(np.int32), np.concatenate(wt)
+        off_k += int(cp[-1])
+    cst.append(np.array([off_e], np.int64))
+    return (np.concatenate(ptr).astype(np.int32), np.concatenate(col).astype(np.int32), np.concatenate(wt),
+            np.concatenate(cst).astype(np.int32), np.concatenate(cpt).astype(np.int32))
 
 
 def _concat(samples):
@@ -318,32 +345,70 @@ class MPNN:
         return [(host[a:b].reshape(ws).copy(), host[b:c].copy()) for (ws, _), (a, b, c) in zip(self.shapes, self.offs)]
 
     # -- device batch ---------------------------------------------------------
-    def _upload(self, samples, with_targets: bool):
+    def _upload(self, samples, with_targets: bool, work=None):
+        """The samples' inputs on the device (features, targets, aggregation
+        stages) and the work buffers of one forward/backward pass.  ``work``
+        (a dict from an earlier upload with at least as many cells and stage
+        rows) lends its buffers, so that several minibatches share them."""
         import torch
         x, layers, t = _concat(samples)
         xn = (x - self.x_mu) / self.x_sd
         d = self._dev
         dev = lambda trip: [torch.from_numpy(np.ascontiguousarray(a)).to(d) for a in trip]
         H = self.hidden
-        g = {"n": x.shape[0], "x": torch.from_numpy(np.ascontiguousarray(xn, np.float32)).to(d), "agg": []}
-        for stages in layers:
+        n = x.shape[0]
+
+        def buf(rows, key, shape_rows):
+            if work is not None and key in work and work[key].shape[0] >= shape_rows:
+                return work[key][:shape_rows]
+            return torch.empty((rows, H), device=d)
+        g = {"n": n, "x": torch.from_numpy(np.ascontiguousarray(xn, np.float32)).to(d), "agg": []}
+        for li, stages in enumerate(layers):
             ag = []
             for k, st in enumerate(stages):
                 last = k == len(stages) - 1
+                wk = None if work is None else work["agg"][li][k]
+                nchM, nchMt = int(st["M"][4][-1]), int(st["Mt"][4][-1])
                 ag.append({"rows": st["rows"], "cols": st["cols"], "M": dev(st["M"]), "Mt": dev(st["Mt"]),
+                           # chunk partials of long rows (none when every row is one chunk)
+                           "pM": torch.empty((nchM, H), device=d) if nchM > st["rows"] else None,
+                           "pMt": torch.empty((nchMt, H), device=d) if nchMt > st["cols"] else None,
+                           "nchM": nchM, "nchMt": nchMt,
                            # forward output of a stage before the last; its gradient
-                           "tmp": None if last else torch.empty((st["rows"], H), device=d),
-                           "gtmp": None if k == 0 else torch.empty((st["cols"], H), device=d)})
+                           "tmp": None if last else (wk["tmp"][:st["rows"]] if wk is not None and wk["tmp"] is not None
+                                                     and wk["tmp"].shape[0] >= st["rows"]
+                                                     else torch.empty((st["rows"], H), device=d)),
+                           "gtmp": None if k == 0 else (wk["gtmp"][:st["cols"]] if wk is not None and wk["gtmp"] is not None
+                                                        and wk["gtmp"].shape[0] >= st["cols"]
+                                                        else torch.empty((st["cols"], H), device=d))})
             g["agg"].append(ag)
         if with_targets:
             tn = (t - self.t_mu) / self.t_sd
             g["t"] = torch.from_numpy(np.ascontiguousarray(tn, np.float32)).to(d)
-        n, H = g["n"], self.hidden
-        g["h"] = [torch.empty((n, H), device=d) for _ in range(self.layers + 1)]
-        g["z"] = [torch.empty((n, H), device=d) for _ in range(self.layers + 1)]
-        g["m"] = [torch.empty((n, H), device=d) for _ in range(self.layers)]
-        g["y"] = torch.empty((n, NOUT), device=d)
+        if work is not None and work["n"] >= n:
+            g["h"] = [a[:n] for a in work["h"]]
+            g["z"] = [a[:n] for a in work["z"]]
+            g["m"] = [a[:n] for a in work["m"]]
+            g["y"] = work["y"][:n]
+            for k in ("wscr", "dh", "dz", "dm", "dy", "mscr"):
+                if work.get(k) is not None:
+                    g[k] = work[k] if k in ("wscr", "mscr") else work[k][:n]
+        else:
+            g["h"] = [torch.empty((n, H), device=d) for _ in range(self.layers + 1)]
+            g["z"] = [torch.empty((n, H), device=d) for _ in range(self.layers + 1)]
+            g["m"] = [torch.empty((n, H), device=d) for _ in range(self.layers)]
+            g["y"] = torch.empty((n, NOUT), device=d)
         return g
+
+    def _spmm(self, M, rows, nch, partial, src, dst, accumulate):
+        """dst (+)= M src over the CSR M: one thread per (row, feature), or in
+        chunks when the matrix has rows longer than one chunk."""
+        L, s, H, P = nat.lib(), self._stream(), self.hidden, self._p
+        if partial is None:
+            nat.check(L.fvdbm_mp_spmm(P(M[0]), P(M[1]), P(M[2]), rows, P(src), H, P(dst), int(accumulate), s))
+        else:
+            nat.check(L.fvdbm_mp_spmm_chunked(P(M[3]), P(M[4]), nch, P(M[1]), P(M[2]), rows, P(src), H, P(dst),
+                                              int(accumulate), P(partial), s))
 
     def _forward(self, g):
         L, s, n, H = nat.lib(), self._stream(), g["n"], self.hidden
@@ -356,7 +421,7 @@ class MPNN:
             for st in g["agg"][l - 1]:
                 dst = st["tmp"] if st["tmp"] is not None else g["m"][l - 1]
                 M = st["M"]
-                nat.check(L.fvdbm_mp_spmm(P(M[0]), P(M[1]), P(M[2]), st["rows"], P(src), H, P(dst), 0, s))
+                self._spmm(M, st["rows"], st["nchM"], st["pM"], src, dst, 0)
                 src = dst
             nat.check(L.fvdbm_mp_dense_fwd(P(hp), H, P(g["m"][l - 1]), H, n, self._w(l), self._b(l), H, 1, P(hp),
                                            P(g["z"][l]), P(g["h"][l]), s))
@@ -364,17 +429,28 @@ class MPNN:
         nat.check(L.fvdbm_mp_dense_fwd(P(g["h"][-1]), H, 0, 0, n, self._w(lo), self._b(lo), NOUT, 0, 0, 0,
                                        P(g["y"]), s))
 
-    def _backward(self, g, dy):
+    def _ensure_work(self, g):
+        """Backward work buffers of g (weight-gradient partials, dh, dz, dm, dy
+        and the loss scratch), sized for its cells."""
         import torch
-        L, s, n, H = nat.lib(), self._stream(), g["n"], self.hidden
-        P = self._p
+        L, n, H = nat.lib(), g["n"], self.hidden
         scratch_n = max(L.fvdbm_mp_wgrad_scratch(n, H, 2 * H), L.fvdbm_mp_wgrad_scratch(n, NOUT, H),
                         L.fvdbm_mp_wgrad_scratch(n, H, NFEAT))
         if g.get("wscr") is None or g["wscr"].numel() * 4 < scratch_n:
             g["wscr"] = torch.empty((scratch_n + 3) // 4, dtype=torch.float32, device=self._dev)
+        if g.get("dh") is None or g["dh"].shape[0] < n:
             g["dh"] = torch.empty((n, H), device=self._dev)
             g["dz"] = torch.empty((n, H), device=self._dev)
             g["dm"] = torch.empty((n, H), device=self._dev)
+        if g.get("dy") is None or g["dy"].shape[0] < n:
+            g["dy"] = torch.empty((n, NOUT), device=self._dev)
+            nb = L.fvdbm_mp_mse_scratch(n * NOUT)
+            g["mscr"] = torch.empty((nb + 7) // 8, dtype=torch.float64, device=self._dev)
+
+    def _backward(self, g, dy):
+        L, s, n, H = nat.lib(), self._stream(), g["n"], self.hidden
+        P = self._p
+        self._ensure_work(g)
         ws, wsn = P(g["wscr"]), g["wscr"].numel() * 4
         lo = self.layers + 1
         G = self.G
@@ -391,10 +467,9 @@ class MPNN:
                 st = g["agg"][l - 1][k]
                 Mt = st["Mt"]
                 if k == 0:  # back to the cells: accumulate into dh
-                    nat.check(L.fvdbm_mp_spmm(P(Mt[0]), P(Mt[1]), P(Mt[2]), st["cols"], P(grad), H, P(g["dh"]), 1, s))
+                    self._spmm(Mt, st["cols"], st["nchMt"], st["pMt"], grad, g["dh"], 1)
                 else:
-                    nat.check(L.fvdbm_mp_spmm(P(Mt[0]), P(Mt[1]), P(Mt[2]), st["cols"], P(grad), H, P(st["gtmp"]),
-                                              0, s))
+                    self._spmm(Mt, st["cols"], st["nchMt"], st["pMt"], grad, st["gtmp"], 0)
                     grad = st["gtmp"]
         nat.check(L.fvdbm_mp_relu_bwd(P(g["dh"]), P(g["z"][0]), P(g["dz"]), n * H, s))
         nat.check(L.fvdbm_mp_dense_bwd_weight(P(g["dz"]), n, H, P(g["x"]), NFEAT, 0, 0, self._w(0, G), self._b(0, G),
@@ -404,10 +479,7 @@ class MPNN:
         """Forward, mean squared error against g['t'] and backward into self.G."""
         import torch
         L, s, n = nat.lib(), self._stream(), g["n"]
-        if g.get("dy") is None:
-            g["dy"] = torch.empty((n, NOUT), device=self._dev)
-            nb = L.fvdbm_mp_mse_scratch(n * NOUT)
-            g["mscr"] = torch.empty((nb + 7) // 8, dtype=torch.float64, device=self._dev)
+        self._ensure_work(g)
         self._forward(g)
         nat.check(L.fvdbm_mp_mse(self._p(g["y"]), self._p(g["t"]), 0, n * NOUT, float(n * NOUT), self._p(g["dy"]),
                                  self._p(g["mscr"]), g["mscr"].numel() * 8, s))
@@ -416,23 +488,47 @@ class MPNN:
 
     # -- training and prediction ------------------------------------------
     def fit(self, samples, epochs: int = 1500, lr: float = 2e-3, lr_final: float = 1e-4, log_every: int = 100,
-            b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8):
-        """Full-batch Adam over all samples (their graphs joined); the learning
-        rate decays geometrically from lr to lr_final.  Returns the loss
-        history [(epoch, loss)]."""
+            b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8, batch_cells: int | None = None):
+        """Adam over the samples (their graphs joined); the learning rate
+        decays geometrically from lr to lr_final.  Full batch by default; with
+        ``batch_cells`` the samples are split, in order, into minibatches of
+        at most that many cells (a sample is never split), uploaded once and
+        stepped in turn, one Adam step each, sharing one set of work buffers.
+        Returns the loss history [(epoch, loss)], the loss of the epoch's last
+        minibatch."""
         x = np.concatenate([s.x for s in samples])
         t = np.concatenate([s.t for s in samples])
         self.x_mu, self.x_sd = x.mean(0), np.maximum(x.std(0), 1e-12)
         self.t_mu, self.t_sd = t.mean(0), np.maximum(t.std(0), 1e-12)
-        g = self._upload(samples, True)
+        groups = [list(samples)]
+        if batch_cells:
+            groups, cur, cells = [], [], 0
+            for smp in samples:
+                if cur and cells + smp.n > batch_cells:
+                    groups.append(cur)
+                    cur, cells = [], 0
+                cur.append(smp)
+                cells += smp.n
+            if cur:
+                groups.append(cur)
+        # the largest minibatch first: its work buffers serve every minibatch
+        order = sorted(range(len(groups)), key=lambda i: -sum(s.n for s in groups[i]))
+        gs = [None] * len(groups)
+        for i in order:
+            gs[i] = self._upload(groups[i], True, work=gs[order[0]])
+            if i == order[0]:
+                self._ensure_work(gs[i])
         L, s = nat.lib(), self._stream()
         hist = []
+        steps = epochs * len(gs)
         for ep in range(epochs):
-            loss = self.loss_and_grads(g)
-            self.step_count += 1
-            rate = lr * (lr_final / lr) ** (ep / max(epochs - 1, 1))
-            nat.check(L.fvdbm_mp_adam(self._p(self.P), self._p(self.M), self._p(self.V), self._p(self.Pb),
-                                      self._p(self.G), self.size, rate, b1, b2, eps, self.step_count, s))
+            for gi, g in enumerate(gs):
+                loss = self.loss_and_grads(g)
+                self.step_count += 1
+                k = ep * len(gs) + gi
+                rate = lr * (lr_final / lr) ** (k / max(steps - 1, 1))
+                nat.check(L.fvdbm_mp_adam(self._p(self.P), self._p(self.M), self._p(self.V), self._p(self.Pb),
+                                          self._p(self.G), self.size, rate, b1, b2, eps, self.step_count, s))
             if ep % log_every == 0 or ep == epochs - 1:
                 hist.append((ep, float(loss.item())))
         return hist
@@ -485,19 +581,28 @@ def macros(pdf):
 
 
 def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, stall_checks: int = 100,
-              stall_factor: float = 0.95):
+              stall_factor: float = 0.95, check_time: float = 0.0):
     """Steps a Batch to steady state with per-case retirement, like
     ``Batch.run_to_steady``, and with the warm-start fallback: when ``init`` =
     (rho [N], vel [N,2]) is given every case starts from feq(rho, u), and a
     case whose residual after ``stall_checks`` checks is not below
     ``stall_factor`` times its value ``stall_checks`` checks earlier restarts
-    from the uniform state feq(1, 0).  Returns per-case steps (including the
-    steps before a restart), status (1 converged, 0 cap, 2 non-finite, 3
-    frozen: residual exactly 0 before the threshold) and the restart flags."""
+    from the uniform state feq(1, 0).  ``check_time`` > 0 takes a case's
+    residual only once it has advanced that much of its own time since its
+    last check (whole chunks of ``check_every`` steps), as
+    ``fvdbm_batch_run_to_steady_time`` does.  Returns per-case steps
+    (including the steps before a restart), status (1 converged, 0 cap, 2
+    non-finite, 3 frozen: residual exactly 0 before the threshold) and the
+    restart flags."""
     S = batch.n_cases
     if init is not None:
         batch.set_cells_eq(*init)
+    dts = np.array([float(d.delta_t) for d in batch.dynamics])
+    window = np.full(S, check_every, np.int64)
+    if check_time > 0:
+        window = np.maximum(1, np.ceil(check_time / dts)).astype(np.int64)
     steps = np.zeros(S, np.int64)
+    since = np.zeros(S, np.int64)
     status = np.zeros(S, np.int32)
     restarted = np.zeros(S, bool)
     active = np.ones(S, bool)
@@ -508,14 +613,20 @@ def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, st
         n = int(min(check_every, np.min(cap - steps[active])))
         batch.step(n)
         steps[active] += n
-        r, _ = batch.residual()
+        since[active] += n
+        take = active & ((since >= window) | (steps >= cap))
+        if not take.any():
+            continue
+        r, _ = batch.residual(take)
         restart = []
-        for s in np.flatnonzero(active):
+        for s in np.flatnonzero(take):
+            since[s] = 0
             hist[s].append(r[s])
             if np.isnan(r[s]):
                 status[s], active[s] = 2, False
-            elif r[s] == 0.0:
-                status[s], active[s] = 3, False
+            elif r[s] == 0.0:  # exact float32 fixed point: converged if it was near the threshold
+                near = len(hist[s]) > 1 and hist[s][-2] < 100.0 * threshold
+                status[s], active[s] = (1 if near else 3), False
             elif r[s] < threshold:
                 status[s], active[s] = 1, False
             elif steps[s] >= cap:
@@ -531,5 +642,6 @@ def run_cases(batch, threshold: float, check_every: int, cap: int, init=None, st
             hist[s] = []
         batch.set_active(active.astype(np.int32))
         if restart:
-            batch.residual()  # new snapshot after the restart
+            batch.residual()  # new snapshots after the restart (every case)
+            since[:] = 0
     return steps, status, restarted

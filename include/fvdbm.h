@@ -72,6 +72,9 @@ extern "C" {
 #define FVDBM_KERNEL_BATCH 6      /* (reported by fvdbm_get_info) packed batch: node BC + fused cell kernel */
 #define FVDBM_KERNEL_FUSED_NODES 7 /* fused cell kernel that also updates the boundary nodes of the
                                       next step (1 kernel) */
+#define FVDBM_KERNEL_PERSIST 8    /* all the steps of one fvdbm_step call in one cooperative launch:
+                                     nodes, grid barrier, cells, grid barrier per step (triangles;
+                                     for meshes whose launches are short) */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {
@@ -284,19 +287,29 @@ int fvdbm_batch_config(void *handle, int32_t block, int32_t prefetch_waves);
 /* Per-case residual and mass (as fvdbm_residual, per case).  [n_cases]. */
 int fvdbm_batch_residual(void *handle, double *res_u, double *mass);
 
+/* The same for the cases with take[s] != 0 only: each over the steps that
+ * case took since its own last residual, whose snapshot is then renewed;
+ * other cases keep their snapshots and their res_u/mass entries are left
+ * as they were.  (The first call after creation or an upload takes every
+ * case.)  [n_cases]. */
+int fvdbm_batch_residual_cases(void *handle, const int32_t *take, double *res_u, double *mass);
+
 /* Mark cases active (1) or retired (0).  A retired case's cells keep their
  * current state in both buffers and are skipped by the step.  [n_cases]. */
 int fvdbm_batch_set_active(void *handle, const int32_t *active);
 
 /* Steps every active case, checking the residuals every check_every steps.
  * A case retires with
- *   FVDBM_CASE_CONVERGED  its residual fell below threshold (and is not 0),
+ *   FVDBM_CASE_CONVERGED  its residual fell below threshold, or reached exactly
+ *                         0 (an exact float32 fixed point) from a previous
+ *                         residual below 100 * threshold,
  *   FVDBM_CASE_NONFINITE  its residual turned NaN (the case diverged),
- *   FVDBM_CASE_FROZEN     its residual is exactly 0: no cell's velocity
- *                         changed over the last check interval, a fixed
- *                         point of the float32 step reached before the
- *                         residual passed the threshold (typically a flow
- *                         that float32 keeps from developing),
+ *   FVDBM_CASE_FROZEN     its residual is exactly 0 (no cell's velocity
+ *                         changed over the last check interval) while the
+ *                         previous one was not below 100 * threshold: the
+ *                         float32 state stopped changing far from
+ *                         convergence (typically a flow that float32 keeps
+ *                         from developing),
  *   FVDBM_CASE_STALLED    its residual set no new minimum in
  *                         FVDBM_STALL_CHECKS consecutive checks,
  *   FVDBM_CASE_CAPPED     it took max_steps[s] steps.

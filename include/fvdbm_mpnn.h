@@ -53,6 +53,15 @@ int fvdbm_mp_relu_bwd(const float *dy, const float *z, float *dz, size_t count, 
 int fvdbm_mp_spmm(const int32_t *row_ptr, const int32_t *col, const float *wt, int32_t n, const float *h,
                   int32_t d, float *out, int32_t accumulate, void *stream);
 
+/* The same for long rows (the coarse-bin means): the entries of each row are
+ * cut into chunks (chunk_start [nchunks+1] entry offsets, chunks never
+ * crossing a row; chunk_ptr [n+1] first chunk of each row); each chunk is
+ * folded in entry order into partial [nchunks][d] (caller's scratch), then
+ * each row folds its chunks in order. */
+int fvdbm_mp_spmm_chunked(const int32_t *chunk_start, const int32_t *chunk_ptr, int32_t nchunks,
+                          const int32_t *col, const float *wt, int32_t n, const float *h, int32_t d, float *out,
+                          int32_t accumulate, float *partial, void *stream);
+
 /* Masked mean squared error: loss = sum mask (y - t)^2 / mask_total into
  * scratch[0] (double, device); dy = 2 mask (y - t) / mask_total.  mask may be
  * NULL (all ones).  scratch: at least fvdbm_mp_mse_scratch(count) bytes. */

@@ -20,7 +20,7 @@ def _cases():
         elif name in D2Q13:
             kernels = ["staged", "fused", "auto"]
         else:
-            kernels = ["one", "tile", "tile_split", "fused", "fused_nodes", "staged"]
+            kernels = ["one", "tile", "tile_split", "fused", "fused_nodes", "persist", "staged"]
         for k in kernels:
             for order in ("none", "rcm", "morton"):
                 out.append((name, k, order))

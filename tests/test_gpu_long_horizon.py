@@ -69,7 +69,7 @@ def test_channel_20000_steps_bitwise(flux):
     pr = OC.Prepared(geo, dyn.inv_tau, dyn.dt32)
     mid = OC.step(geo, st, dyn.inv_tau, dyn.dt32, n_steps=10_000, prepared=pr)
     ref = OC.step(geo, mid, dyn.inv_tau, dyn.dt32, n_steps=10_000, prepared=pr)
-    for kernel in ("auto", "fused_nodes", "staged"):
+    for kernel in ("auto", "fused_nodes", "persist", "staged"):
         env = Environment(c, f, n, kernel=kernel)
         env.init()
         env.step(10_000)

@@ -12,7 +12,7 @@ import oracle_np as O
 
 pytestmark = pytest.mark.gpu
 
-KERNELS = {"D2Q9": ("one", "tile", "tile_split", "fused", "fused_nodes", "staged"),
+KERNELS = {"D2Q9": ("one", "tile", "tile_split", "fused", "fused_nodes", "persist", "staged"),
            "D2Q13": ("staged", "fused")}
 KEYS = ("cells_pdf", "cells_rho", "cells_vel", "cells_pdf_eq", "faces_pdf", "nodes_pdf", "nodes_rho", "nodes_vel")
 SPECIAL = np.array([np.nan, np.inf, -np.inf, 3.0e38, -3.0e38, 1.0e-40, -1.0e-40, 0.0, -0.0, 1.0e20, 1.0e-30],
