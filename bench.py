@@ -14,6 +14,12 @@ write-back of the flush data): each timed step reads its inputs from HBM.  Each 
 on the library's stream; the cell kernel (the dominant one) is timed on its
 own for the roofline.
 
+The timed family is ``--kernel`` (default ``fast``: the single-launch step
+with contracted float32 arithmetic, bitwise reproducible run to run and as
+close to the float64 step as the reference's own float32 step); the
+bit-exact default family of ``Environment`` is timed beside it on the same
+mesh under ``bitexact``.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Under torchrun (N>1) every rank runs an independent replica (a differently
@@ -54,8 +60,8 @@ def parse():
     ap.add_argument("--no-above-l2", action="store_true",
                     help="skip the ~4M-triangle point whose per-step traffic is well above L2")
     ap.add_argument("--e2e-steps", type=int, default=100)
-    ap.add_argument("--kernel", default="auto",
-                    choices=["auto", "one", "fused", "fused_nodes", "persist", "staged", "tile", "tile_split"])
+    ap.add_argument("--kernel", default="fast",
+                    choices=["auto", "one", "fused", "fused_nodes", "fast", "persist", "staged", "tile", "tile_split"])
     # --workload batch: time-to-steady of many independent cases, batched vs one at a time
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--threshold", type=float, default=1e-6)
@@ -135,13 +141,17 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel_key):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+def profiled_traffic(kernel, desc):
+    """DRAM bytes per launch of a kernel on this workload from the committed
+    ncu summary, if one was captured for it."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
-            return json.load(fh).get(kernel_key)
+            rec = json.load(fh).get(kernel, {})
     except Exception:
         return None
+    if rec.get("workload") != desc.get("workload") or rec.get("flux") != desc.get("flux"):
+        return None
+    return rec.get("bytes_per_launch")
 
 
 class ClockSampler:
@@ -314,13 +324,48 @@ def above_l2_point(args, local, flush_l2_on):
     N = info["n_cells"]
     env.close()
     return {"workload": desc["workload"], "cells": N, "faces": info["n_faces"], "bytes_per_step": B,
-            "l2_bytes": L2_BYTES, "kernel": "k_fused_nodes" if info["kernel"] == 7 else str(info["kernel"]),
+            "l2_bytes": L2_BYTES, "kernel": {7: "k_fused_nodes", 9: "k_fused_nodes_fast"}.get(info["kernel"], str(info["kernel"])),
             "flushed": {"us_per_step": round(flushed_us, 3), "mcups": round(N / flushed_us, 1),
                         "frac": round(B / flushed_us / 1e3 / peak, 4), "steps": K},
             "consecutive": {"us_per_step": round(cons_us, 3), "mcups": round(N / cons_us, 1),
                             "frac": round(B / cons_us / 1e3 / peak, 4), "steps": steps,
                             "note": "graph replay without a flush; the step's inputs are 3.6x the L2"},
             "peak": peak, "peak_kind": peak_kind}
+
+
+def bitexact_point(args, local, flush_l2, c, f, n, K, desc):
+    """The bit-exact default family (what ``Environment`` runs unless told
+    otherwise) on the same mesh and protocol: K single steps, L2 flushed
+    before each, each bracketed by CUDA events on the library's stream."""
+    import torch
+
+    from fvdbm_jax_gb300 import Environment
+    from fvdbm_jax_gb300 import _native as nat
+    env = Environment(c, f, n, device=local, kernel="auto")
+    env.init()
+    info = env.info()
+    L = nat.lib()
+    h = env.handle
+    stream = torch.cuda.ExternalStream(env.stream_ptr, device=f"cuda:{local}")
+    env.step(max(args.warmup, 3))
+    env.sync()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
+    for k in range(K):
+        with torch.cuda.stream(stream):
+            flush_l2(k)
+        ev[k][0].record(stream)
+        nat.check(L.fvdbm_step(h, 1), h)
+        ev[k][1].record(stream)
+    env.sync()
+    us = statistics.mean(e[0].elapsed_time(e[1]) for e in ev) * 1e3
+    peak, peak_kind = measured_peaks()
+    N, B = info["n_cells"], info["bytes_per_step"]
+    env.close()
+    assert info["launches_per_step"] == 1
+    return {"kernel": {7: "k_fused_nodes"}.get(info["kernel"], str(info["kernel"])),
+            "note": "bit for bit with the reference's step; the same flushed protocol",
+            "avg_launch_us": round(us, 3), "mcups": round(N / us, 1),
+            "frac": round(B / us / 1e3 / peak, 4), "traffic": profiled_traffic("k_fused_nodes", desc), "steps": K}
 
 
 def run_reference(args):
@@ -420,7 +465,7 @@ def run_gb300(args):
     # kernel does the whole step in one launch.
     F = info["n_faces"]
     K3 = int(np.asarray(c.face_indices).shape[1])
-    if info["kernel"] in (3, 5, 7, 8):
+    if info["kernel"] in (3, 5, 7, 8, 9):
         cell_bytes = info["bytes_per_step"]
     elif info["kernel"] == 4:
         cell_bytes = info["bytes_per_step"] - 36.0 * info["n_bc_nodes"]
@@ -466,6 +511,9 @@ def run_gb300(args):
     above = None
     if rank == 0 and args.workload == "porous1m" and not args.no_above_l2:
         above = above_l2_point(args, local, flush_l2)
+    exact = None
+    if rank == 0 and info["kernel"] == nat.KERNEL_FAST:
+        exact = bitexact_point(args, local, flush_l2, c, f, n, Kp, desc)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -478,22 +526,28 @@ def run_gb300(args):
                          "sample": f"{ndone} whole steps ({nel:.1f}s) of the vectorised numpy restatement, "
                                    f"whole-array gathers and folds as the reference's XLA CPU program does"}}
 
+    kname = {1: "k_gather", 2: "k_fused", 3: "k_tile", 4: "k_tile", 5: "k_step",
+             7: "k_fused_nodes", 8: "k_persist", 9: "k_fused_nodes_fast"}[info["kernel"]]
     if rank == 0:
         desc.update({"global_cells": int(cells_all), "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                      "l2": "flushed between timed steps (2x L2 written, then read back, on the step's stream)",
                      "kernel": {1: "staged", 2: "fused", 3: "tile", 4: "tile_split", 5: "one",
-                                7: "fused_nodes", 8: "persist"}[info["kernel"]],
+                                7: "fused_nodes", 8: "persist", 9: "fast"}[info["kernel"]],
                      "launches_per_step": info["launches_per_step"],
                      "ctas_per_sm": info["ctas_per_sm"]})
+        if info["kernel"] == nat.KERNEL_FAST:
+            desc["arithmetic"] = ("contracted float32 (multiply-adds, reciprocals of the lattice constants, "
+                                  "compact face slots): bitwise reproducible run to run, as close to the float64 "
+                                  "step as the reference's float32 step (tests/test_gpu_fast.py); the bit-exact "
+                                  "default family is timed beside it under 'bitexact'")
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "MCUPS", "n_gpus": ws, "steps": K,
             "warmup": args.warmup, "ms_per_step": round(total_ms_max / K, 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": desc,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": profiled_traffic("cell_kernel"),
-                         "kernel": {1: "k_gather", 2: "k_fused", 3: "k_tile", 4: "k_tile", 5: "k_step",
-                                    7: "k_fused_nodes", 8: "k_persist"}[info["kernel"]],
+                         "frac": round(achieved / peak, 4), "traffic": profiled_traffic(kname, desc),
+                         "kernel": kname,
                          "bytes_per_launch": cell_bytes, "avg_launch_us": round(cell_avg_s * 1e6, 3),
                          "peak_kind": peak_kind,
                          "step_frac": round(step_achieved / peak, 4),
@@ -513,6 +567,8 @@ def run_gb300(args):
         }
         if above is not None:
             line["above_l2"] = above
+        if exact is not None:
+            line["bitexact"] = exact
         print(json.dumps(line), flush=True)
     env.close()
     if ws > 1:

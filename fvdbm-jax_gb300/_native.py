@@ -17,7 +17,7 @@ FVDBM_UPWIND, FVDBM_LAX_WENDROFF = 0, 1
 VARIANT_NONE, VARIANT_FACE_SCALE, VARIANT_FACE_Q_SCALE = 0, 1, 2
 ORDER_NONE, ORDER_RCM, ORDER_MORTON = 0, 1, 2
 KERNEL_AUTO, KERNEL_STAGED, KERNEL_FUSED, KERNEL_TILE, KERNEL_TILE_SPLIT, KERNEL_ONE = 0, 1, 2, 3, 4, 5
-KERNEL_BATCH, KERNEL_FUSED_NODES, KERNEL_PERSIST = 6, 7, 8
+KERNEL_BATCH, KERNEL_FUSED_NODES, KERNEL_PERSIST, KERNEL_FAST = 6, 7, 8, 9
 
 _i32p = C.POINTER(C.c_int32)
 _f32p = C.POINTER(C.c_float)

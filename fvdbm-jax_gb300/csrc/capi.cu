@@ -461,12 +461,13 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   DevPlan& p = h->dp;
   // the fused kernels take three face slots per cell (triangles)
   h->fused = hp.fusable && hp.K == 3 && params->kernel != FVDBM_KERNEL_STAGED;
-  if (params->kernel == FVDBM_KERNEL_FUSED_NODES && !(hp.fusable && hp.K == 3 && hp.stencil_first)) {
+  const bool want_fnodes = params->kernel == FVDBM_KERNEL_FUSED_NODES || params->kernel == FVDBM_KERNEL_FAST;
+  if (want_fnodes && !(hp.fusable && hp.K == 3 && hp.stencil_first)) {
     h->err = "the in-kernel node update needs triangles (3 face slots per cell), every cell face slot "
              "naming a face of that cell, and no per-q flux scale";
     return create_fail(h, FVDBM_EINVAL);
   }
-  h->fnodes = params->kernel == FVDBM_KERNEL_FUSED_NODES ||
+  h->fnodes = want_fnodes ||
               (auto_family && pplan.kernel == FVDBM_KERNEL_FUSED_NODES && hp.fusable && hp.K == 3 && hp.stencil_first);
   if (hp.q == 13) {
     // D2Q13 (d2q13.cu): the staged kernels, or on triangles the node kernel
@@ -548,6 +549,7 @@ static int create_impl(const fvdbm_mesh_t* mesh, const fvdbm_params_t* params, c
   } else {
     p.d_c6x2 = p.d_c2x2;  // (unused by D2Q9; keeps the conditions below uniform)
   }
+  p.fast = hp.fast ? 1 : 0;
   p.cdiv_mode = (p.d_c2.ok && p.d_c4x2.ok && p.d_c2x2.ok && p.d_c6x2.ok)
                     ? ((p.d_c2.two && p.d_c4x2.two && p.d_c2x2.two && p.d_c6x2.two) ? 2 : 1)
                     : 0;
@@ -1395,7 +1397,8 @@ int fvdbm_get_info(void* handle, fvdbm_info_t* info) {
   info->n_nodes = hp.P;
   info->n_bc_nodes = hp.Mc;
   info->n_ghost_faces = hp.n_ghost_faces;
-  info->kernel = h->persist ? FVDBM_KERNEL_PERSIST : h->fnodes ? FVDBM_KERNEL_FUSED_NODES
+  info->kernel = h->persist ? FVDBM_KERNEL_PERSIST
+               : h->fnodes ? (h->dp.fast ? FVDBM_KERNEL_FAST : FVDBM_KERNEL_FUSED_NODES)
                : h->batch ? FVDBM_KERNEL_BATCH : h->one ? FVDBM_KERNEL_ONE
                          : h->tile ? (h->dp.tile_nodes ? FVDBM_KERNEL_TILE : FVDBM_KERNEL_TILE_SPLIT)
                                    : (h->fused ? FVDBM_KERNEL_FUSED : FVDBM_KERNEL_STAGED);

@@ -45,6 +45,23 @@ struct HfRows {
   __host__ __device__ constexpr int rows() const { return (4 + (scheme == 1 ? 2 : 0) + (variant == 1 ? 1 : 0)) * K; }
 };
 
+// Rows of the fast family's compact half faces (FVDBM_KERNEL_FAST): per slot
+// the code word, a = n * (L*sigma) (times the face scale of FACE_SCALE, times
+// 1/area in finite-volume mode) as two rows, and for Lax-Wendroff the
+// interpolation weight r and g = dt / (D2 * L*sigma [* scale] [/ area]).  In
+// the upwind code word HF_SLOT1 is then slot1 XOR (L*sigma < 0): the upwind
+// side of direction q is this cell's exactly when xi_q . a >= 0 (xi_q . a == 0
+// carries no flux).
+struct HfFastRows {
+  int K, scheme;
+  __host__ __device__ constexpr int code(int k) const { return k; }
+  __host__ __device__ constexpr int ax(int k) const { return K + k; }
+  __host__ __device__ constexpr int ay(int k) const { return 2 * K + k; }
+  __host__ __device__ constexpr int r(int k) const { return 3 * K + k; }
+  __host__ __device__ constexpr int g(int k) const { return 4 * K + k; }
+  __host__ __device__ constexpr int rows() const { return (3 + (scheme == 1 ? 2 : 0)) * K; }
+};
+
 // Node-cell entry: cell index (device numbering); bit 31 marks an entry whose
 // reference index was -1 (its rho/vel gather wraps to the last cell but its
 // non-equilibrium part is zero, src/containers.py:388-390).
@@ -57,6 +74,7 @@ struct HostPlan {
   int scheme = 0, variant = 0;
   int q = 9;  // lattice velocities
   bool fv = false;
+  bool fast = false;  // compact half faces of the fast family
   bool fusable = false;
   int ordering = 0;
 
@@ -176,6 +194,7 @@ struct DevPlan {
   int q;       // lattice velocities: 9 or 13
   CDiv d_c2, d_c4x2, d_c2x2, d_c6x2;  // d_c6x2: D2Q13 only
   int cdiv_mode;  // 2: the lattice's divisors' two-operation forms verified, 1: five-operation, 0: neither
+  int fast;       // FVDBM_KERNEL_FAST: contracted arithmetic in the fused cell update
   // staged faces
   const int* fs0;
   const int* fs1;

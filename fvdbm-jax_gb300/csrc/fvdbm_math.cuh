@@ -304,6 +304,45 @@ __device__ __forceinline__ float feq_one(float rho, float ux, float uy, int q, c
   return (c_W[q] * rho) * s;
 }
 
+// ---------------------------------------------------------------------------
+// Contracted forms for the fast family (FVDBM_KERNEL_FAST).  Not the
+// reference's rounding: explicit multiply-adds, multiplications by the
+// rounded reciprocals of the lattice constants, an approximate reciprocal of
+// rho, and no literal paths for non-finite values (NaN/inf propagate, but not
+// with the reference's signs).  The evaluation order is fixed, so a step is
+// still bitwise reproducible run to run; against the reference the step
+// differs by a few float32 ulps per cell.
+
+// rho = sum_q f_q (pairwise), u = (KSI^T f) * (1/rho)
+__device__ __forceinline__ void macros_fast(const float f[Q], float& rho, float& ux, float& uy) {
+  rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+  const float mx = ((f[1] - f[3]) + (f[5] - f[6])) + (f[8] - f[7]);
+  const float my = ((f[2] - f[4]) + (f[5] + f[6])) - (f[7] + f[8]);
+  const float ir = __fdividef(1.0f, rho);
+  ux = mx * ir;
+  uy = my * ir;
+}
+
+// feq_q = W_q rho (1 - u.u/(2C^2) + a_q/C^2 + a_q^2/(2C^4)), a_q = xi_q . u,
+// with the constants' reciprocals ic2 = 1/C^2, ic4x2 = 1/(2C^4), ic2x2 = 1/(2C^2)
+__device__ __forceinline__ void feq9_fast(float rho, float ux, float uy, float ic2, float ic4x2, float ic2x2,
+                                          float out[Q]) {
+  const float base = __fmaf_rn(-__fmaf_rn(ux, ux, __fmul_rn(uy, uy)), ic2x2, 1.0f);
+  const float w0 = c_W[0] * rho, w1 = c_W[1] * rho, w5 = c_W[5] * rho;
+  const float a[4] = {ux, uy, ux + uy, uy - ux};
+  out[0] = w0 * base;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float b = __fmaf_rn(__fmul_rn(a[j], a[j]), ic4x2, base);
+    const float c = __fmul_rn(a[j], ic2);
+    const float w = j < 2 ? w1 : w5;
+    // directions (1, 3), (2, 4), (5, 7), (6, 8): +a and -a
+    const int qp = j < 2 ? 1 + j : 5 + (j - 2);
+    out[qp] = w * (b + c);
+    out[qp + 2] = w * (b - c);
+  }
+}
+
 // v_q = xi_q . n (src/containers.py:235); symmetric form for finite n
 __device__ __forceinline__ void xi_dot_n(float nx, float ny, bool finite_n, float v[Q]) {
   if (!finite_n) {

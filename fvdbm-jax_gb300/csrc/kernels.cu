@@ -416,6 +416,109 @@ __device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __rest
   fused_cell_f<SCHEME, VARIANT, FV, GHOST_CG, RECORD>(p, fin, fout, i, f, code, nx, ny, Ls, hb, p.inv_tau, p.dt);
 }
 
+// ---------------------------------------------------------------------------
+// The fast family's cell update (FVDBM_KERNEL_FAST): the same step with
+// contracted arithmetic (fvdbm_math.cuh, "contracted forms").  Direction q = 0
+// has xi.n = 0 and carries no flux; the pairs (1, 3), (2, 4), (5, 7), (6, 8)
+// share |xi.n|, so one comparison picks both upwind sides (at xi.n = 0 the
+// choice does not matter: the flux is zero either way).
+__device__ __forceinline__ void face_other_fast(const DevPlan& p, const float* __restrict__ fin, int code,
+                                                const float f[Q], float o[Q]) {
+  const int other = code >> HF_SHIFT;
+  if (code & HF_GHOST) {
+    const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
+    const float rg = __ldg(p.gh_r + other);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const float mq = (__ldg(p.node_pdf + size_t(q) * p.Mp + a) + __ldg(p.node_pdf + size_t(q) * p.Mp + b)) * 0.5f;
+      o[q] = __fmaf_rn(mq - f[q], rg, mq);
+    }
+  } else {
+    load_cell(fin, other, o);
+  }
+}
+
+// Flux of one face slot from the compact slot: a = n * (L*sigma [*scale]
+// [/area]) per face slot (HfFastRows), so that xi_q . a is the flux
+// coefficient of direction q and its sign picks the upwind side.
+template <int SCHEME>
+__device__ __forceinline__ void face_flux_fast(int code, float ax, float ay, float r, float g, const float f[Q],
+                                               const float o[Q], float acc[Q]) {
+  const bool slot1 = (code & HF_SLOT1) != 0;
+  const float a4[4] = {ax, ay, ax + ay, ay - ax};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int qp = j < 2 ? 1 + j : 5 + (j - 2), qm = qp + 2;  // xi.a = +a4[j], -a4[j]
+    float pp, pm;
+    if (SCHEME == 0) {
+      const bool up = (a4[j] >= 0.0f) != slot1;
+      pp = up ? f[qp] : o[qp];
+      pm = up ? o[qm] : f[qm];
+    } else {
+      // Lax-Wendroff: phi = l + (r - l) * (d0/(d0+d1) - (xi.n) dt/(2(d0+d1))),
+      // (xi.n) dt/(2(d0+d1)) = (xi.a) * g
+      const float lp = slot1 ? o[qp] : f[qp], rp = slot1 ? f[qp] : o[qp];
+      const float lm = slot1 ? o[qm] : f[qm], rm = slot1 ? f[qm] : o[qm];
+      pp = __fmaf_rn(rp - lp, __fmaf_rn(-a4[j], g, r), lp);
+      pm = __fmaf_rn(rm - lm, __fmaf_rn(a4[j], g, r), lm);
+    }
+    acc[qp] = __fmaf_rn(pp, a4[j], acc[qp]);
+    acc[qm] = __fmaf_rn(-pm, a4[j], acc[qm]);
+  }
+}
+
+template <int SCHEME>
+__device__ __forceinline__ void load_slots_fast(const DevPlan& p, int i, const unsigned*& hb, int code[3],
+                                                float ax[3], float ay[3]) {
+  constexpr int HROWS = (3 + (SCHEME == 1 ? 2 : 0)) * 3;
+  const HfFastRows HX{3, SCHEME};
+  hb = p.hf + cell_base(i < p.N ? i : 0, HROWS);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    code[k] = int(__ldg(hb + HX.code(k) * 32));
+    ax[k] = __uint_as_float(__ldg(hb + HX.ax(k) * 32));
+    ay[k] = __uint_as_float(__ldg(hb + HX.ay(k) * 32));
+  }
+}
+
+template <int SCHEME>
+__device__ __forceinline__ void fused_cell_fast(const DevPlan& p, const float* __restrict__ fin,
+                                                float* __restrict__ fout, int i, const int code[3],
+                                                const float ax[3], const float ay[3],
+                                                const unsigned* __restrict__ hb) {
+  const HfFastRows HX{3, SCHEME};
+  float f[Q];
+  load_cell(fin, i, f);
+  float acc[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) acc[q] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float o[Q];
+    face_other_fast(p, fin, code[k], f, o);
+    float r = 0.0f, g = 0.0f;
+    if (SCHEME == 1) {
+      r = __uint_as_float(__ldg(hb + HX.r(k) * 32));
+      g = __uint_as_float(__ldg(hb + HX.g(k) * 32));
+    }
+    face_flux_fast<SCHEME>(code[k], ax[k], ay[k], r, g, f, o, acc);
+  }
+  float rho, ux, uy, eq[Q];
+  macros_fast(f, rho, ux, uy);
+  feq9_fast(rho, ux, uy, p.d_c2.zr, p.d_c4x2.zr, p.d_c2x2.zr, eq);
+  // f + dt*(inv_tau*(eq - f) - acc) (acc already carries 1/area in
+  // finite-volume mode)
+  const float om = p.dt * p.inv_tau;
+  float* out = fout + cell_base(i, Q);
+  float fn[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    fn[q] = __fmaf_rn(-p.dt, acc[q], __fmaf_rn(om, eq[q] - f[q], f[q]));
+    out[q * 32] = fn[q];
+  }
+  if (i >= p.stencil_start && i < p.stencil_end) record_stencil(p, i, fn);
+}
+
 template <int SCHEME, int VARIANT>
 __device__ __forceinline__ void load_slots(const DevPlan& p, int i, const unsigned*& hb, int code[3],
                                            float nx[3], float ny[3], float Ls[3]) {
@@ -465,11 +568,11 @@ __global__ void __launch_bounds__(256) k_fused(DevPlan p, const float* __restric
 // buffers, written by the previous launch.  The last node block to finish
 // resets the two counters for the next launch.  At most NB blocks wait, far
 // fewer than the resident blocks, so the recording blocks always get an SM.
-template <int SCHEME, int VARIANT, bool FV>
-__global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __restrict__ fin,
-                                                     float* __restrict__ fout, int R, int node_at,
-                                                     int prefetch_blocks) {
-  constexpr int HROWS = (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
+template <int SCHEME, int VARIANT, bool FV, bool FAST>
+__device__ __forceinline__ void fused_nodes_block(const DevPlan& p, const float* __restrict__ fin,
+                                                  float* __restrict__ fout, int R, int node_at,
+                                                  int prefetch_blocks) {
+  constexpr int HROWS = FAST ? (3 + (SCHEME == 1 ? 2 : 0)) * 3 : (4 + (SCHEME == 1 ? 2 : 0) + (VARIANT == 1 ? 1 : 0)) * 3;
   static_assert(NODE_BLOCK_ENTRIES == 256, "node blocks use the whole CTA");
   __shared__ float prod[12][NODE_BLOCK_ENTRIES];
   __shared__ float lastm[3];
@@ -506,11 +609,19 @@ __global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __r
   const int i = cb * 256 + threadIdx.x;
   const unsigned* hb;
   int code[3];
-  float nx[3], ny[3], Ls[3];
-  load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
-  grid_dep_wait();  // fin and the node pdfs come from the previous launch
-  if (pf_cells > 0) prefetch_l2(fin + size_t(ahead) * 256 * Q, pf_cells * Q * sizeof(float));
-  if (i < p.N) fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
+  if constexpr (FAST) {
+    float ax[3], ay[3];
+    load_slots_fast<SCHEME>(p, i, hb, code, ax, ay);
+    grid_dep_wait();  // fin and the node pdfs come from the previous launch
+    if (pf_cells > 0) prefetch_l2(fin + size_t(ahead) * 256 * Q, pf_cells * Q * sizeof(float));
+    if (i < p.N) fused_cell_fast<SCHEME>(p, fin, fout, i, code, ax, ay, hb);
+  } else {
+    float nx[3], ny[3], Ls[3];
+    load_slots<SCHEME, VARIANT>(p, i, hb, code, nx, ny, Ls);
+    grid_dep_wait();  // fin and the node pdfs come from the previous launch
+    if (pf_cells > 0) prefetch_l2(fin + size_t(ahead) * 256 * Q, pf_cells * Q * sizeof(float));
+    if (i < p.N) fused_cell<SCHEME, VARIANT, FV, false, true>(p, fin, fout, i, code, nx, ny, Ls, hb);
+  }
   if (cb < R) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -518,6 +629,27 @@ __global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __r
       atomicAdd(&ctr[0], 1);
     }
   }
+}
+
+template <int SCHEME, int VARIANT, bool FV>
+__global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __restrict__ fin,
+                                                     float* __restrict__ fout, int R, int node_at,
+                                                     int prefetch_blocks) {
+  fused_nodes_block<SCHEME, VARIANT, FV, false>(p, fin, fout, R, node_at, prefetch_blocks);
+}
+
+// The fast family's launch: the same blocks with the contracted cell update
+// on the compact half faces (the face scale and 1/area are folded into them,
+// so only the flux scheme is a template parameter).  Five resident blocks per
+// SM (48 registers) measured faster than six (40 registers, with spills).
+#ifndef FVDBM_FAST_MIN_BLOCKS
+#define FVDBM_FAST_MIN_BLOCKS 5
+#endif
+template <int SCHEME>
+__global__ void __launch_bounds__(256, FVDBM_FAST_MIN_BLOCKS)
+    k_fused_nodes_fast(DevPlan p, const float* __restrict__ fin, float* __restrict__ fout, int R, int node_at,
+                       int prefetch_blocks) {
+  fused_nodes_block<SCHEME, 0, false, true>(p, fin, fout, R, node_at, prefetch_blocks);
 }
 
 // ---------------------------------------------------------------------------
@@ -1050,9 +1182,10 @@ static cudaError_t fused_nodes_dispatch(const DevPlan& p, const float* fin, floa
   // recording blocks and 37.4 us at the end)
   const int node_at = std::min(ncb, std::max(R, ncb * 3 / 4));
   const int pf = fused_prefetch_blocks();
-  if (p.fv)
-    return launch_ex(k_fused_nodes<S, V, true>, ncb + p.NB, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
-  return launch_ex(k_fused_nodes<S, V, false>, ncb + p.NB, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
+  const int g = ncb + p.NB;
+  if (p.fast) return launch_ex(k_fused_nodes_fast<S>, g, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
+  if (p.fv) return launch_ex(k_fused_nodes<S, V, true>, g, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
+  return launch_ex(k_fused_nodes<S, V, false>, g, 256, 0, s, pdl, p, fin, fout, R, node_at, pf);
 }
 
 cudaError_t launch_fused_nodes(const DevPlan& p, const float* fin, float* fout, cudaStream_t s, bool pdl) {

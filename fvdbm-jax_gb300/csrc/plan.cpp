@@ -164,6 +164,8 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
   if (pr.flux_scheme != FVDBM_UPWIND && pr.flux_scheme != FVDBM_LAX_WENDROFF)
     return "Unknown flux scheme";
   if (pr.variant < 0 || pr.variant > 2) return "unknown flux variant";
+  if (pr.kernel < FVDBM_KERNEL_AUTO || pr.kernel > FVDBM_KERNEL_FAST || pr.kernel == FVDBM_KERNEL_BATCH)
+    return "unknown kernel family";
   hp.q = pr.lattice == 0 ? 9 : pr.lattice;
   if (hp.q != 9 && hp.q != 13) return "lattice must be 9 (D2Q9) or 13 (D2Q13)";
   if (hp.q == 13 && pr.variant != 0) return "D2Q13 takes no flux-scale variant";
@@ -287,7 +289,7 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
   // read its macros).
   hp.stencil_start = N;
   hp.stencil_end = N;
-  hp.stencil_first = pr.kernel == FVDBM_KERNEL_FUSED_NODES && !segs;
+  hp.stencil_first = (pr.kernel == FVDBM_KERNEL_FUSED_NODES || pr.kernel == FVDBM_KERNEL_FAST) && !segs;
   if (N > 0 && Kn > 0 && pr.kernel != FVDBM_KERNEL_TILE && !segs) {
     std::vector<char> member(N, 0);
     bool padded = false;
@@ -516,7 +518,9 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
       }
     }
   const HfRows HR{K, pr.flux_scheme, pr.variant};
-  hp.hrows = HR.rows();
+  const HfFastRows HX{K, pr.flux_scheme};
+  hp.fast = pr.kernel == FVDBM_KERNEL_FAST && !segs;
+  hp.hrows = hp.fast ? HX.rows() : HR.rows();
   auto hfi = [&](int i, int row) { return size_t(i >> 5) * size_t(hp.hrows) * 32 + size_t(row) * 32 + (i & 31); };
   auto fbits = [](float x) {
     uint32_t u;
@@ -525,7 +529,7 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
   };
   if (hp.fusable) {
     hp.hf.assign(size_t(hp.Np / 32) * hp.hrows * 32, 0u);
-    if (pr.flux_scheme == FVDBM_LAX_WENDROFF)
+    if (pr.flux_scheme == FVDBM_LAX_WENDROFF && !hp.fast)
       for (int i = 0; i < hp.Np; ++i)
         for (int k = 0; k < K; ++k) hp.hf[hfi(i, HR.d2(k))] = fbits(1.0f);
   }
@@ -551,6 +555,22 @@ std::string build_plan(const void* mesh_v, const void* params_v, HostPlan& hp, c
         code |= HF_GHOST | (g << HF_SHIFT);
       } else {
         code |= hp.cell_new[oth] << HF_SHIFT;
+      }
+      if (hp.fast) {
+        // a = n * (L*sigma [*scale] [/area]), rounded once from double
+        double s = double(hp.fL[j]) * double(sg);
+        if (pr.variant == 1) s *= double(hp.fscale[j]);
+        if (hp.fv) s *= double(m.cell_inv_area[c]);
+        if (pr.flux_scheme == FVDBM_UPWIND) code = (code & ~HF_SLOT1) | (slot1 != (s < 0.0) ? HF_SLOT1 : 0);
+        hp.hf[hfi(i, HX.code(k))] = uint32_t(code);
+        hp.hf[hfi(i, HX.ax(k))] = fbits(float(double(hp.fnx[j]) * s));
+        hp.hf[hfi(i, HX.ay(k))] = fbits(float(double(hp.fny[j]) * s));
+        if (pr.flux_scheme == FVDBM_LAX_WENDROFF) {
+          hp.hf[hfi(i, HX.r(k))] = fbits(hp.fr[j]);
+          const double den = double(hp.fD2[j]) * s;
+          hp.hf[hfi(i, HX.g(k))] = fbits(den != 0.0 ? float(double(pr.delta_t) / den) : 0.0f);
+        }
+        continue;
       }
       hp.hf[hfi(i, HR.code(k))] = uint32_t(code);
       hp.hf[hfi(i, HR.nx(k))] = fbits(hp.fnx[j]);

@@ -34,7 +34,8 @@ F32, I32 = np.float32, np.int32
 _ORDER = {"none": nat.ORDER_NONE, "rcm": nat.ORDER_RCM, "morton": nat.ORDER_MORTON}
 _KERNEL = {"auto": nat.KERNEL_AUTO, "staged": nat.KERNEL_STAGED, "fused": nat.KERNEL_FUSED,
            "tile": nat.KERNEL_TILE, "tile_split": nat.KERNEL_TILE_SPLIT, "one": nat.KERNEL_ONE,
-           "fused_nodes": nat.KERNEL_FUSED_NODES, "persist": nat.KERNEL_PERSIST}
+           "fused_nodes": nat.KERNEL_FUSED_NODES, "persist": nat.KERNEL_PERSIST,
+           "fast": nat.KERNEL_FAST}
 
 
 def _face_scale(faces):

@@ -75,6 +75,11 @@ extern "C" {
 #define FVDBM_KERNEL_PERSIST 8    /* all the steps of one fvdbm_step call in one cooperative launch:
                                      nodes, grid barrier, cells, grid barrier per step (triangles;
                                      for meshes whose launches are short) */
+#define FVDBM_KERNEL_FAST 9       /* FUSED_NODES with contracted float32 arithmetic (multiply-adds,
+                                     reciprocals of the lattice constants, no literal paths for
+                                     non-finite values): bitwise reproducible run to run, within a
+                                     few float32 ulps per step of the reference's rounding, not
+                                     bitwise equal to it (D2Q9 triangles; never picked by AUTO) */
 
 /* Reference-layout mesh (host pointers).  N cells, F faces, P nodes. */
 typedef struct fvdbm_mesh {

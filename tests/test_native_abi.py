@@ -34,6 +34,18 @@ def test_library_exports_every_declared_symbol():
     assert L.fvdbm_abi_version() == 4
 
 
+def test_kernel_family_constants_match_the_header():
+    src = open(os.path.join(os.path.dirname(HEADERS[0]), "fvdbm.h")).read()
+    defs = {k: int(v) for k, v in re.findall(r"#define FVDBM_(KERNEL_\w+)\s+(\d+)", src)}
+    assert defs["KERNEL_FAST"] == 9
+    for k, v in defs.items():
+        if hasattr(nat, k):
+            assert getattr(nat, k) == v, k
+    from fvdbm_jax_gb300.environment import _KERNEL
+    assert _KERNEL["fast"] == defs["KERNEL_FAST"]
+    assert _KERNEL["fused_nodes"] == defs["KERNEL_FUSED_NODES"]
+
+
 def _tiny_mesh(**over):
     # two triangles sharing face 0; faces 1-4 are boundary faces
     a = dict(
@@ -47,13 +59,13 @@ def _tiny_mesh(**over):
     return a
 
 
-def _create(a, scheme=0):
+def _create(a, scheme=0, kernel=0):
     L = nat.lib()
     m = nat.Mesh(a["cfi"].shape[0], a["fc"].shape[0], a["nt"].shape[0], a["cfi"].shape[1], a["nc"].shape[1],
                  nat.iptr(a["cfi"]), nat.iptr(a["cfs"]), nat.iptr(a["fc"]), nat.fptr(a["fd"]), nat.iptr(a["fnd"]),
                  nat.fptr(a["fn"]), nat.fptr(a["fL"]), None, nat.iptr(a["nt"]), nat.iptr(a["nc"]),
                  nat.fptr(a["nd"]), None, None)
-    p = nat.Params(scheme, 0, 1.0, 0.1, 1 / 3, 2 / 9, 2 / 3, 0, 0, 0)
+    p = nat.Params(scheme, 0, 1.0, 0.1, 1 / 3, 2 / 9, 2 / 3, 0, kernel, 0)
     h = C.c_void_p()
     rc = L.fvdbm_create(C.byref(m), C.byref(p), C.byref(h))
     if rc == 0:
@@ -76,6 +88,12 @@ def test_invalid_containers_are_rejected(over, needle):
 def test_unknown_scheme_rejected():
     rc, msg = _create(_tiny_mesh(), scheme=7)
     assert rc == nat_EINVAL() and "Unknown flux scheme" in msg
+
+
+@pytest.mark.parametrize("kernel", [-1, 6, 10, 42])
+def test_unknown_kernel_family_rejected(kernel):
+    rc, msg = _create(_tiny_mesh(), kernel=kernel)
+    assert rc == nat_EINVAL() and "unknown kernel family" in msg
 
 
 def nat_EINVAL():
