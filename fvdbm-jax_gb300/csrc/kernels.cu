@@ -467,6 +467,50 @@ __device__ __forceinline__ void face_flux_fast(int code, float ax, float ay, flo
   }
 }
 
+// Upwind flux of one compact face slot, reading only the pdfs it uses: of
+// each direction pair (q, opposite q) with xi.a = +a, -a exactly one takes
+// the value across the face (the inflow one), so a face needs 4 values of
+// the neighbour (or of the ghost), not 9, at a row that varies by lane.
+__device__ __forceinline__ void face_upwind_fast(const DevPlan& p, const float* __restrict__ fin, int code,
+                                                 float ax, float ay, const float f[Q], float acc[Q]) {
+  const int other = code >> HF_SHIFT;
+  const bool slot1 = (code & HF_SLOT1) != 0;
+  const float a4[4] = {ax, ay, ax + ay, ay - ax};
+  bool up[4];
+  int qn[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int qp = j < 2 ? 1 + j : 5 + (j - 2);
+    up[j] = (a4[j] >= 0.0f) != slot1;  // qp flows out (this cell's value), qp + 2 flows in
+    qn[j] = up[j] ? qp + 2 : qp;
+  }
+  float o4[4];
+  if (code & HF_GHOST) {
+    const int a = __ldg(p.gh_a + other), b = __ldg(p.gh_b + other);
+    const float rg = __ldg(p.gh_r + other);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int qp = j < 2 ? 1 + j : 5 + (j - 2);
+      const float fq = up[j] ? f[qp + 2] : f[qp];
+      const float* np_ = p.node_pdf + size_t(qn[j]) * p.Mp;
+      const float mq = (__ldg(np_ + a) + __ldg(np_ + b)) * 0.5f;
+      o4[j] = __fmaf_rn(mq - fq, rg, mq);
+    }
+  } else {
+    const float* b = fin + cell_base(other, Q);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) o4[j] = __ldg(b + qn[j] * 32);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int qp = j < 2 ? 1 + j : 5 + (j - 2), qm = qp + 2;
+    const float pp = up[j] ? f[qp] : o4[j];
+    const float pm = up[j] ? o4[j] : f[qm];
+    acc[qp] = __fmaf_rn(pp, a4[j], acc[qp]);
+    acc[qm] = __fmaf_rn(-pm, a4[j], acc[qm]);
+  }
+}
+
 template <int SCHEME>
 __device__ __forceinline__ void load_slots_fast(const DevPlan& p, int i, const unsigned*& hb, int code[3],
                                                 float ax[3], float ay[3]) {
@@ -494,14 +538,15 @@ __device__ __forceinline__ void fused_cell_fast(const DevPlan& p, const float* _
   for (int q = 0; q < Q; ++q) acc[q] = 0.0f;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    float o[Q];
-    face_other_fast(p, fin, code[k], f, o);
-    float r = 0.0f, g = 0.0f;
-    if (SCHEME == 1) {
-      r = __uint_as_float(__ldg(hb + HX.r(k) * 32));
-      g = __uint_as_float(__ldg(hb + HX.g(k) * 32));
+    if (SCHEME == 0) {
+      face_upwind_fast(p, fin, code[k], ax[k], ay[k], f, acc);
+    } else {
+      float o[Q];
+      face_other_fast(p, fin, code[k], f, o);
+      const float r = __uint_as_float(__ldg(hb + HX.r(k) * 32));
+      const float g = __uint_as_float(__ldg(hb + HX.g(k) * 32));
+      face_flux_fast<SCHEME>(code[k], ax[k], ay[k], r, g, f, o, acc);
     }
-    face_flux_fast<SCHEME>(code[k], ax[k], ay[k], r, g, f, o, acc);
   }
   float rho, ux, uy, eq[Q];
   macros_fast(f, rho, ux, uy);
@@ -640,8 +685,11 @@ __global__ void __launch_bounds__(256) k_fused_nodes(DevPlan p, const float* __r
 
 // The fast family's launch: the same blocks with the contracted cell update
 // on the compact half faces (the face scale and 1/area are folded into them,
-// so only the flux scheme is a template parameter).  Five resident blocks per
-// SM (48 registers) measured faster than six (40 registers, with spills).
+// so only the flux scheme is a template parameter).  On the 1M step five
+// resident blocks per SM (48 registers) measured 26.9 us per launch, four
+// 28.8 us and six (40 registers, with spills) 27.8 us; the L2 prefetch
+// distance of the bit-exact kernel (two blocks per SM ahead) 26.9 us against
+// 27.2 (none), 27.9 (four) and 28.5 us (six).
 #ifndef FVDBM_FAST_MIN_BLOCKS
 #define FVDBM_FAST_MIN_BLOCKS 5
 #endif
