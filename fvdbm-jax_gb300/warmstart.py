@@ -135,15 +135,30 @@ def wall_distance(mesher, faces, nodes):
     return cKDTree(mid).query(cen)[0]
 
 
-def potential(mesher, cells, faces, nodes, rho_in: float, rho_out: float):
-    """A potential-flow estimate of the flow pattern: phi solves the cell
-    Laplacian with phi = (rho - rho_out)/(rho_in - rho_out) on open boundary
-    faces (both end nodes density nodes) and no flux through walls, face
-    conductances L/(d0 + d1) (L/d0 to a boundary face); its Green-Gauss
-    gradient points along the channels the steady flow takes.  Returns phi
-    and grad phi per cell (zeros when the mesh has no open boundary)."""
+class PotentialSystem:
+    """The potential-flow estimate of one case as a linear problem: the cell
+    Laplacian A phi = rhs (A symmetric positive definite on every part of the
+    mesh that touches an open boundary, CSR float32) and the affine map from
+    phi to its Green-Gauss gradient, grad phi = (Gx phi + g0x, Gy phi + g0y)."""
+
+    def __init__(self, A, rhs, Gx, Gy, g0x, g0y):
+        self.A, self.rhs, self.Gx, self.Gy, self.g0x, self.g0y = A, rhs, Gx, Gy, g0x, g0y
+        self.n = A.shape[0]
+
+    def gradient(self, phi):
+        phi = np.asarray(phi, np.float64)
+        return self.Gx @ phi + self.g0x, self.Gy @ phi + self.g0y
+
+
+def potential_system(mesher, cells, faces, nodes, rho_in: float, rho_out: float):
+    """The system of ``potential``: phi = (rho - rho_out)/(rho_in - rho_out)
+    on open boundary faces (both end nodes density nodes), no flux through
+    walls, face conductances L/(d0 + d1) (L/d0 to a boundary face).  Face
+    values of phi: linear between the two cells, the boundary value on open
+    faces, the owner's value on walls; the gradient is
+    sum_k sign_k phi_f n_f L_f / A per cell.  None when the mesh has no open
+    boundary."""
     import scipy.sparse as sp
-    import scipy.sparse.linalg as spl
     fc = np.asarray(faces.stencil_cells_index, np.int64)
     sd = np.asarray(faces.stencil_dists, np.float64)
     L = np.asarray(faces.L, np.float64).reshape(-1)
@@ -151,14 +166,14 @@ def potential(mesher, cells, faces, nodes, rho_in: float, rho_out: float):
     t = np.asarray(nodes.type).reshape(-1)
     nr = np.asarray(nodes.rho, np.float64).reshape(-1)
     ncell = np.asarray(mesher.cell_centers).shape[0]
+    F = fc.shape[0]
     inner = (fc[:, 0] >= 0) & (fc[:, 1] >= 0)
     bnd = ~inner
     open_ = bnd & (t[fn[:, 0]] == 2) & (t[fn[:, 1]] == 2)
     if not open_.any():
-        z = np.zeros(ncell)
-        return z, z, z
+        return None
     d = max(rho_in - rho_out, 1e-30)
-    phib = np.zeros(fc.shape[0])
+    phib = np.zeros(F)
     phib[open_] = 0.5 * ((nr[fn[open_, 0]] - rho_out) + (nr[fn[open_, 1]] - rho_out)) / d
     w_in = L[inner] / np.maximum(sd[inner, 0] + sd[inner, 1], 1e-30)
     a, b = fc[inner, 0], fc[inner, 1]
@@ -168,37 +183,120 @@ def potential(mesher, cells, faces, nodes, rho_in: float, rho_out: float):
     diag = np.bincount(a, w_in, ncell) + np.bincount(b, w_in, ncell) + np.bincount(ob, w_bd, ncell)
     A = sp.coo_matrix((np.concatenate([-w_in, -w_in, diag]),
                        (np.concatenate([a, b, np.arange(ncell)]), np.concatenate([b, a, np.arange(ncell)]))),
-                      shape=(ncell, ncell)).tocsc()
+                      shape=(ncell, ncell)).tocsr()
+    A.sum_duplicates()
+    A.sort_indices()
     rhs = np.bincount(ob, w_bd * phib[open_], ncell)
-    phi = spl.spsolve(A, rhs)
-    # face values: linear between the two cells, the boundary value on open
-    # faces, the owner's value on walls; then sum_k sign_k phi_f n_f L_f / A
-    pf = np.empty(fc.shape[0])
+    # face values pf = P phi + pf0
+    fin = np.nonzero(inner)[0]
     d0, d1 = sd[inner, 0], sd[inner, 1]
-    pf[inner] = (phi[a] * d1 + phi[b] * d0) / np.maximum(d0 + d1, 1e-30)
-    pf[bnd] = phi[owner[bnd]]
-    pf[open_] = phib[open_]
+    den = np.maximum(d0 + d1, 1e-30)
+    wall = np.nonzero(bnd & ~open_)[0]
+    P = sp.csr_matrix((np.concatenate([d1 / den, d0 / den, np.ones(wall.size)]),
+                       (np.concatenate([fin, fin, wall]), np.concatenate([a, b, owner[wall]]))), shape=(F, ncell))
+    pf0 = np.where(open_, phib, 0.0)
+    # gradient rows: C[c, f] = sign * n * L / area over the cell's face slots
     n = np.asarray(faces.n, np.float64)
     cf = np.asarray(cells.face_indices, np.int64)
     cs = np.asarray(cells.face_normals, np.float64)
     area = np.asarray(mesher.cell_areas, np.float64).reshape(-1)
     ok = cf >= 0
     fi = np.where(ok, cf, 0)
-    contrib = (cs * ok)[:, :, None] * (pf[fi] * L[fi])[:, :, None] * n[fi]
-    g = contrib.sum(1) / area[:, None]
-    return phi, g[:, 0], g[:, 1]
+    rows = np.repeat(np.arange(ncell), cf.shape[1])
+    base = ((cs * ok) * L[fi] / area[:, None]).reshape(-1)
+    fcol = fi.reshape(-1)
+    Cx = sp.csr_matrix((base * n[fcol, 0], (rows, fcol)), shape=(ncell, F))
+    Cy = sp.csr_matrix((base * n[fcol, 1], (rows, fcol)), shape=(ncell, F))
+    return PotentialSystem(A, rhs, (Cx @ P).tocsr(), (Cy @ P).tocsr(), Cx @ pf0, Cy @ pf0)
 
 
-def features(mesher, cells, faces, nodes, rho_in: float, rho_out: float) -> np.ndarray:
+def potential(mesher, cells, faces, nodes, rho_in: float, rho_out: float):
+    """A potential-flow estimate of the flow pattern (``potential_system``),
+    solved on the host by a sparse direct solver: phi and grad phi per cell
+    (zeros when the mesh has no open boundary).  Its gradient points along
+    the channels the steady flow takes.  ``solve_potentials`` solves the same
+    systems on the GPU."""
+    import scipy.sparse.linalg as spl
+    ps = potential_system(mesher, cells, faces, nodes, rho_in, rho_out)
+    if ps is None:
+        z = np.zeros(np.asarray(mesher.cell_centers).shape[0])
+        return z, z, z
+    phi = spl.spsolve(ps.A.tocsc(), ps.rhs)
+    gx, gy = ps.gradient(phi)
+    return phi, gx, gy
+
+
+def features(mesher, cells, faces, nodes, rho_in: float, rho_out: float, phi=None) -> np.ndarray:
     """Per cell: centroid, wall distance, area, inlet and outlet density, and
-    the potential-flow estimate phi, grad phi."""
+    the potential-flow estimate phi, grad phi (columns 6-8).  phi: False
+    leaves those three columns zero (``sample(..., defer_potential=True)``)."""
     cen = np.asarray(mesher.cell_centers, np.float64)
     area = np.asarray(mesher.cell_areas, np.float64).reshape(-1)
     wd = wall_distance(mesher, faces, nodes)
     n = cen.shape[0]
-    phi, gx, gy = potential(mesher, cells, faces, nodes, rho_in, rho_out)
-    return np.stack([cen[:, 0], cen[:, 1], wd, area, np.full(n, rho_in), np.full(n, rho_out), phi, -gx, -gy],
+    if phi is False:
+        ph = gx = gy = np.zeros(n)
+    else:
+        ph, gx, gy = potential(mesher, cells, faces, nodes, rho_in, rho_out)
+    return np.stack([cen[:, 0], cen[:, 1], wd, area, np.full(n, rho_in), np.full(n, rho_out), ph, -gx, -gy],
                     1).astype(np.float32)
+
+
+def solve_potentials(samples, device: int = 0, rtol: float = 1e-6, max_iter: int = 50_000,
+                     check_every: int = 100):
+    """Fill the potential-flow columns of the samples built with
+    ``defer_potential=True``: their systems are solved together on the GPU as
+    one block-diagonal system (``fvdbm_pcg``: Jacobi-preconditioned
+    conjugate gradients, float32 vectors, float64 fixed-order dot products),
+    then each gradient is formed on the host.  Returns (iterations, relative
+    residual)."""
+    import ctypes as C
+
+    import torch
+    pend = [s for s in samples if getattr(s, "pending", None) is not None]
+    if not pend:
+        return 0, 0.0
+    off, ip, ix, vals, rhs = 0, [np.zeros(1, np.int64)], [], [], []
+    nnz = 0
+    for s in pend:
+        A = s.pending.A
+        ip.append(A.indptr[1:].astype(np.int64) + nnz)
+        ix.append(A.indices.astype(np.int64) + off)
+        vals.append(A.data)
+        rhs.append(s.pending.rhs)
+        off += A.shape[0]
+        nnz += A.nnz
+    if off >= 2 ** 31 or nnz >= 2 ** 31:
+        raise ValueError("potential systems too large for one solve (2^31 unknowns or entries)")
+    dev = torch.device(f"cuda:{device}")
+    t_ip = torch.from_numpy(np.concatenate(ip).astype(np.int32)).to(dev)
+    t_ix = torch.from_numpy(np.concatenate(ix).astype(np.int32)).to(dev)
+    t_v = torch.from_numpy(np.concatenate(vals).astype(np.float32)).to(dev)
+    t_b = torch.from_numpy(np.concatenate(rhs).astype(np.float32)).to(dev)
+    t_x = torch.zeros(off, dtype=torch.float32, device=dev)
+    L = nat.lib()
+    wb = int(L.fvdbm_pcg_work_bytes(off))
+    work = torch.empty(wb, dtype=torch.uint8, device=dev)
+    it, rel = C.c_int32(0), C.c_double(0.0)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    rc = L.fvdbm_pcg(off, t_ip.data_ptr(), t_ix.data_ptr(), t_v.data_ptr(), t_b.data_ptr(), t_x.data_ptr(),
+                     int(max_iter), float(rtol), int(check_every), work.data_ptr(), wb, st, C.byref(it), C.byref(rel))
+    if rc != 0:
+        raise nat.FvdbmError(f"fvdbm_pcg failed ({rc})")
+    if not np.isfinite(rel.value):
+        raise nat.FvdbmError("fvdbm_pcg: non-finite residual (matrix not positive definite?)")
+    x = t_x.cpu().numpy().astype(np.float64)
+    o = 0
+    for s in pend:
+        ps = s.pending
+        phi = x[o:o + ps.n]
+        o += ps.n
+        gx, gy = ps.gradient(phi)
+        s.x[:, 6] = phi
+        s.x[:, 7] = -gx
+        s.x[:, 8] = -gy
+        s.pending = None
+    return int(it.value), float(rel.value)
 
 
 def targets(rho, vel, rho_in: float, rho_out: float) -> np.ndarray:
@@ -218,11 +316,12 @@ class Sample:
     """One case for the network: features, per-layer aggregation stages and
     (for training) targets."""
 
-    def __init__(self, x, aggs, t=None):
+    def __init__(self, x, aggs, t=None, pending=None):
         self.x = np.asarray(x, np.float32)
         self.aggs = aggs
         self.t = None if t is None else np.asarray(t, np.float32)
         self.n = self.x.shape[0]
+        self.pending = pending  # PotentialSystem still to solve (solve_potentials)
 
 
 def _cat_csr(mats, rows, cols):
@@ -351,6 +450,8 @@ class MPNN:
         (a dict from an earlier upload with at least as many cells and stage
         rows) lends its buffers, so that several minibatches share them."""
         import torch
+        if any(getattr(s, "pending", None) is not None for s in samples):
+            raise ValueError("a sample's potential-flow system is unsolved: call solve_potentials first")
         x, layers, t = _concat(samples)
         xn = (x - self.x_mu) / self.x_sd
         d = self._dev
@@ -496,6 +597,8 @@ class MPNN:
         stepped in turn, one Adam step each, sharing one set of work buffers.
         Returns the loss history [(epoch, loss)], the loss of the epoch's last
         minibatch."""
+        if any(getattr(s, "pending", None) is not None for s in samples):
+            raise ValueError("a sample's potential-flow system is unsolved: call solve_potentials first")
         x = np.concatenate([s.x for s in samples])
         t = np.concatenate([s.t for s in samples])
         self.x_mu, self.x_sd = x.mean(0), np.maximum(x.std(0), 1e-12)
@@ -563,13 +666,21 @@ class MPNN:
 
 # ----------------------------------------------------------------------------
 # solver side
-def sample(case, rho_in: float, rho_out: float, rho=None, vel=None, scales=SCALES) -> Sample:
+def sample(case, rho_in: float, rho_out: float, rho=None, vel=None, scales=SCALES,
+           defer_potential: bool = False) -> Sample:
     """Sample of a case (dynamics, cells, faces, nodes, mesher); with the
-    steady rho/vel it carries the training targets."""
+    steady rho/vel it carries the training targets.  defer_potential: leave
+    the potential-flow system unsolved (``solve_potentials`` solves many on
+    the GPU at once); else it is solved here on the host."""
     dyn, c, f, n, m = case
-    x = features(m, c, f, n, rho_in, rho_out)
+    pend = None
+    if defer_potential:
+        x = features(m, c, f, n, rho_in, rho_out, phi=False)
+        pend = potential_system(m, c, f, n, rho_in, rho_out)
+    else:
+        x = features(m, c, f, n, rho_in, rho_out)
     t = None if rho is None else targets(rho, vel, rho_in, rho_out)
-    return Sample(x, aggregations(f, m.cell_centers, x.shape[0], scales), t)
+    return Sample(x, aggregations(f, m.cell_centers, x.shape[0], scales), t, pending=pend)
 
 
 def macros(pdf):

@@ -77,6 +77,21 @@ int fvdbm_mp_adam(float *w, float *m, float *v, uint16_t *wb, const float *g, si
 /* y = x rounded to bfloat16 (nearest even). */
 int fvdbm_mp_to_bf16(const float *x, uint16_t *y, size_t count, void *stream);
 
+/* Features: Jacobi-preconditioned conjugate gradients for A x = b, A
+ * symmetric positive definite in CSR (indptr [n+1], indices in [0, n),
+ * float32 values; the warm start's potential-flow estimate solves one cell
+ * Laplacian per case, many cases as one block-diagonal system).  x holds the
+ * initial guess on entry and the solution on return.  Iterates until
+ * ||r|| <= rtol ||b|| (tested every check_every iterations, where the call
+ * synchronises the stream) or max_iter.  Dot products are summed in double
+ * in a fixed order: bitwise reproducible.  work: device scratch of at least
+ * fvdbm_pcg_work_bytes(n) bytes.  *iters and *rel_res report the end state
+ * (rel_res NaN: A was not positive definite or the input not finite). */
+size_t fvdbm_pcg_work_bytes(int32_t n);
+int fvdbm_pcg(int32_t n, const int32_t *indptr, const int32_t *indices, const float *values, const float *b,
+              float *x, int32_t max_iter, double rtol, int32_t check_every, void *work, size_t work_bytes,
+              void *stream, int32_t *iters, double *rel_res);
+
 #ifdef __cplusplus
 }
 #endif
