@@ -774,8 +774,8 @@ def run_warmstart(args):
     pcg_s = time.perf_counter() - t2
     feat_s = time.perf_counter() - t
     t = time.perf_counter()
-    for smp, sp in zip(esamples, espec):
-        r, v = WS.untarget(net.predict(smp), sp["rho_in"], sp["rho_out"])
+    for y, sp in zip(net.predict_many(esamples), espec):
+        r, v = WS.untarget(y, sp["rho_in"], sp["rho_out"])
         rho.append(r)
         vel.append(v)
     infer_s = time.perf_counter() - t + feat_s

@@ -647,6 +647,32 @@ class MPNN:
         y = g["y"].detach().cpu().numpy()
         return y * self.t_sd + self.t_mu
 
+    def predict_many(self, samples, batch_cells: int = 2_000_000):
+        """Network outputs of several samples (target units) [N_i,3] each:
+        the samples are joined into groups of at most ``batch_cells`` cells
+        (a sample is never split), one forward pass per group, all groups on
+        the work buffers of the largest."""
+        groups, cur, cells = [], [], 0
+        for smp in samples:
+            if cur and cells + smp.n > batch_cells:
+                groups.append(cur)
+                cur, cells = [], 0
+            cur.append(smp)
+            cells += smp.n
+        if cur:
+            groups.append(cur)
+        order = sorted(range(len(groups)), key=lambda i: -sum(s.n for s in groups[i]))
+        outs = [None] * len(groups)
+        work = None
+        for i in order:
+            g = self._upload(groups[i], False, work=work)
+            if work is None:
+                work = g
+            self._forward(g)
+            y = g["y"].detach().cpu().numpy()[:sum(s.n for s in groups[i])]
+            outs[i] = np.split(y * self.t_sd + self.t_mu, np.cumsum([s.n for s in groups[i]])[:-1])
+        return [y for grp in outs for y in grp]
+
     def save(self, path):
         np.savez(path, P=self.P.detach().cpu().numpy(), x_mu=self.x_mu, x_sd=self.x_sd, t_mu=self.t_mu,
                  t_sd=self.t_sd, hidden=self.hidden, layers=self.layers, scales=np.array([str(s) for s in self.scales]))

@@ -47,3 +47,17 @@ def test_unsolved_samples_are_refused():
     net = WS.MPNN(seed=0)
     with pytest.raises(ValueError, match="solve_potentials"):
         net.fit([s], epochs=1)
+
+
+def test_predict_many_equals_predict():
+    from fvdbm_jax_gb300 import warmstart as WS
+    cs = _cases()
+    smp = [WS.sample(case, rin, rout, defer_potential=True) for case, rin, rout in cs]
+    WS.solve_potentials(smp)
+    net = WS.MPNN(seed=3)
+    one = [net.predict(s) for s in smp]
+    for bc in (10**9, 20_000):  # one group; several groups on shared buffers
+        many = net.predict_many(smp, batch_cells=bc)
+        assert len(many) == len(one)
+        for a, b in zip(one, many):
+            assert np.array_equal(a, b)
