@@ -64,6 +64,9 @@ def parse():
                     choices=["auto", "one", "fused", "fused_nodes", "fast", "persist", "staged", "tile", "tile_split"])
     # --workload batch: time-to-steady of many independent cases, batched vs one at a time
     ap.add_argument("--cases", type=int, default=256)
+    ap.add_argument("--units", default="lattice", choices=["lattice", "unit"],
+                    help="--workload batch: lattice units (mesh spacing ~1, the reference's update and "
+                         "tau = 3UL/Re + 1/2) or the unit square (finite-volume update, tau = 3UL/Re)")
     ap.add_argument("--threshold", type=float, default=1e-6)
     ap.add_argument("--check-every", type=int, default=100)
     ap.add_argument("--check-time", type=float, default=5.0,
@@ -584,12 +587,16 @@ def run_batch(args):
     per-case check windows.  Set-up (meshing, plans, autotuning) is outside
     both timings.
 
-    Regime: the finite-volume scaled update (flux sum / cell area), tau from
-    Re by the discrete Boltzmann equation's nu = c_s^2 tau (tau = 3 U L / Re,
-    U = 0.1, L = 1), dt = min(area / perimeter, tau) per case, porous inlet /
-    outlet densities 1.05 / 0.95 (tests/porous_flow.ipynb:470-474).  A case's
-    residual is taken over at least ``--check-time`` units of its own time,
-    which keeps float32 rounding noise below the threshold."""
+    Regime (``--units lattice``, the default): every case meshed at a
+    spacing of about 1, the reference's own update (no division by the cell
+    area), tau = 3 U L / Re + 1/2 with U = 0.1 and L the case's side in those
+    units (the notebooks' convention, tests/flow_over_cyl.ipynb:216),
+    dt = 0.5 min edge; porous inlet / outlet densities 1.05 / 0.95
+    (tests/porous_flow.ipynb:470-474).  ``--units unit``: the unit square,
+    the finite-volume scaled update, tau = 3 U L / Re with L = 1 and
+    dt = min(area / perimeter, tau).  A case's residual is taken over at
+    least ``--check-time`` units of its own time, which keeps float32
+    rounding noise below the threshold."""
     import numpy as np
     import torch
 
@@ -600,9 +607,12 @@ def run_batch(args):
     t0 = time.perf_counter()
     n_cav = args.cases // 2
     # several GPUs: the cases are split (greedy by size), no exchange at all
+    lattice = args.units == "lattice"
+    fv = not lattice
     suite, desc = CS.batch_suite(seed=0, n_cavity=n_cav, n_porous=args.cases - n_cav, flux=args.flux,
                                  workers=min(16, os.cpu_count() or 1), rank=rank, n_ranks=ws,
-                                 fv_dt=1.0, rho_in=1.05, rho_out=0.95, tau_rule="dbm")
+                                 fv_dt=None if lattice else 1.0, rho_in=1.05, rho_out=0.95,
+                                 tau_rule="notebook" if lattice else "dbm", units=args.units)
     torch.cuda.set_device(local)
     setup_s = time.perf_counter() - t0
     cells = np.array([d["cells"] for d in desc], np.int64)
@@ -611,7 +621,7 @@ def run_batch(args):
     window = np.array([int(np.ceil(max(1, int(np.ceil(args.check_time / d["dt"]))) / every)) * every
                        for d in desc], np.int64)
 
-    b = Batch([(c, f, n) for _, c, f, n in suite], device=local, finite_volume=True)
+    b = Batch([(c, f, n) for _, c, f, n in suite], device=local, finite_volume=fv)
     b.init()
     tune = b.autotune(steps=32)
     b.sync()
@@ -625,7 +635,7 @@ def run_batch(args):
 
     steps_p, plain_s = [], 0.0
     for (_, c, f, n), w in zip(suite, window):
-        env = Environment(c, f, n, device=local, finite_volume=True)
+        env = Environment(c, f, n, device=local, finite_volume=fv)
         env.init()
         env.sync()
         t = time.perf_counter()
@@ -661,8 +671,12 @@ def run_batch(args):
             "autotune": tune,
             "config": {"workload": f"{args.cases} independent cases: {n_cav} lid cavities (2k-60k cells, lid 0.1), "
                                    f"{args.cases - n_cav} porous squares (10k-120k cells, 20-200 obstacles, "
-                                   "rho 1.05 / 0.95), Re 50-400 via tau = 3UL/Re, finite-volume update, "
-                                   "dt = min(area/perimeter, tau)", "cells": int(all_cells), "flux": args.flux,
+                                   "rho 1.05 / 0.95), Re 50-400; " + (
+                                       "lattice units (mesh spacing ~1), tau = 3UL/Re + 1/2 with L the side "
+                                       "in cells, the reference's update, dt = 0.5 min edge" if lattice else
+                                       "unit square, tau = 3UL/Re, finite-volume update, "
+                                       "dt = min(area/perimeter, tau)"),
+                       "units": args.units, "cells": int(all_cells), "flux": args.flux,
                        "check_every": every, "check_time": args.check_time, "step_cap": cap,
                        "setup_s": round(setup_s, 1)}}
     print(json.dumps(line), flush=True)

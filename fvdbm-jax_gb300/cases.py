@@ -27,10 +27,25 @@ def tau_from_re(re: float, u: float = LID_U, length: float = 1.0, rule: str = "n
     return 3.0 * u * length / re + 0.5
 
 
-def _mesher(raw):
+def _mesher(raw, scale: float = 1.0):
+    """Mesher of a raw mesh whose coordinates are multiplied by ``scale``."""
+    if scale != 1.0:
+        raw.points = np.asarray(raw.points, np.float64) * float(scale)
     m = Mesher().import_meshpy(raw)
     m.calc_mesh_properties()
     return m
+
+
+def cavity_lattice_scale(n: int) -> float:
+    """Scale that puts the n x n cavity grid at spacing 1 (lattice units: the
+    domain side is n - 1)."""
+    return float(n - 1)
+
+
+def porous_lattice_scale(n_target: int, porosity: float) -> float:
+    """Scale that puts the porous square's mesh spacing (``meshgen.porous``)
+    at about 1 (lattice units: the domain side is the scale)."""
+    return float(1.0 / np.sqrt(4.0 * porosity / (np.sqrt(3.0) * n_target)))
 
 
 def fv_stable_dt(m, factor: float = 1.0) -> float:
@@ -55,11 +70,12 @@ def _dt(m, dt_scale, delta_t, fv_dt, tau=None):
 
 
 def lid_cavity(n: int = 41, tau: float = 0.6, flux: str = "upwind", dt_scale: float = 0.5,
-               lid: float = LID_U, seed: int = 0, mesher: bool = False, fv_dt: float | None = None):
-    """Unit square from an n x n jittered grid; lid (marker 3) moving at
-    ``lid``, other walls at rest; dt = dt_scale * min edge, or
+               lid: float = LID_U, seed: int = 0, mesher: bool = False, fv_dt: float | None = None,
+               scale: float = 1.0):
+    """Unit square from an n x n jittered grid (side ``scale``); lid (marker
+    3) moving at ``lid``, other walls at rest; dt = dt_scale * min edge, or
     ``fv_stable_dt(m, fv_dt)`` when fv_dt is given (finite-volume mode)."""
-    m = _mesher(meshgen.cavity(n, seed=seed))
+    m = _mesher(meshgen.cavity(n, seed=seed), scale)
     dyn = D2Q9(tau, _dt(m, dt_scale, None, fv_dt, tau))
     c, f, nd = m.to_env(dyn, flux)
     for mk in (1, 2, 4):
@@ -71,8 +87,8 @@ def lid_cavity(n: int = 41, tau: float = 0.6, flux: str = "upwind", dt_scale: fl
 def porous_square(n_obstacles: int = 400, n_target: int = 1_000_000, tau: float = 0.6,
                   rho_in: float = 1.001, rho_out: float = 1.0, porosity: float = 0.70,
                   flux: str = "upwind", dt_scale: float = 0.5, delta_t: float | None = None,
-                  seed: int = 0, mesher: bool = False, fv_dt: float | None = None):
-    """Porous unit square: inlet density rho_in (left, marker 4), outlet
+                  seed: int = 0, mesher: bool = False, fv_dt: float | None = None, scale: float = 1.0):
+    """Porous unit square (side ``scale``): inlet density rho_in (left, marker 4), outlet
     rho_out (right, marker 2), no-slip walls and obstacles.  dt is ``delta_t``
     when given, else ``fv_stable_dt(m, fv_dt)`` when fv_dt is given, else
     dt_scale * min edge.  When the obstacles do not fit with the default
@@ -87,7 +103,7 @@ def porous_square(n_obstacles: int = 400, n_target: int = 1_000_000, tau: float 
             continue
     if raw is None:
         raise RuntimeError("could not place the obstacles")
-    m = _mesher(raw)
+    m = _mesher(raw, scale)
     dyn = D2Q9(tau, _dt(m, dt_scale, delta_t, fv_dt, tau))
     c, f, nd = m.to_env(dyn, flux)
     for mk in (1, 3, 5):
@@ -99,11 +115,12 @@ def porous_square(n_obstacles: int = 400, n_target: int = 1_000_000, tau: float 
 
 def _make(spec):
     fv = spec.get("fv_dt")
+    sc = spec.get("scale", 1.0)
     if spec["kind"] == "cavity":
-        return lid_cavity(spec["grid"], spec["tau"], spec["flux"], seed=spec["seed"], fv_dt=fv)
+        return lid_cavity(spec["grid"], spec["tau"], spec["flux"], seed=spec["seed"], fv_dt=fv, scale=sc)
     return porous_square(spec["obstacles"], spec["n_target"], spec["tau"], porosity=spec["porosity"],
                          flux=spec["flux"], seed=spec["seed"], fv_dt=fv,
-                         rho_in=spec.get("rho_in", 1.001), rho_out=spec.get("rho_out", 1.0))
+                         rho_in=spec.get("rho_in", 1.001), rho_out=spec.get("rho_out", 1.0), scale=sc)
 
 
 def partition_cases(costs, n_parts: int):
@@ -124,7 +141,7 @@ def batch_suite(seed: int = 0, n_cavity: int = 128, n_porous: int = 128, flux: s
                 cavity_cells=(2_000, 60_000), porous_cells=(10_000, 120_000), obstacles=(20, 200),
                 re=(50.0, 400.0), porosity: float = 0.8, workers: int = 0, rank: int = 0, n_ranks: int = 1,
                 fv_dt: float | None = None, rho_in: float = 1.001, rho_out: float = 1.0,
-                tau_rule: str = "notebook"):
+                tau_rule: str = "notebook", units: str = "unit"):
     """Independent cases of uneven size and Reynolds number: cavities with
     N uniform in ``cavity_cells`` (grid n from N = 2(n-1)^2) and porous squares
     with N uniform in ``porous_cells`` and an obstacle count uniform in
@@ -136,21 +153,30 @@ def batch_suite(seed: int = 0, n_cavity: int = 128, n_porous: int = 128, flux: s
     and returned.  ``fv_dt`` sets every case's dt to ``fv_stable_dt(m,
     fv_dt)`` (for finite-volume mode, at most tau); ``rho_in``/``rho_out``
     are the porous cases' inlet and outlet densities; ``tau_rule`` is the
-    Re -> tau rule of ``tau_from_re``."""
+    Re -> tau rule of ``tau_from_re``.  ``units``: "unit" meshes every case
+    on the unit square (Re with L = 1); "lattice" scales each case so that its
+    mesh spacing is about 1 (``cavity_lattice_scale``,
+    ``porous_lattice_scale``) and takes L = the scaled side, the units the
+    reference's notebooks use (tau = 3 U L / Re + 1/2 with L in cells)."""
+    if units not in ("unit", "lattice"):
+        raise ValueError("units must be 'unit' or 'lattice'")
     rng = np.random.default_rng(seed)
     specs = []
     for i in range(n_cavity):
         N = rng.uniform(*cavity_cells)
         r = float(rng.uniform(*re))
-        specs.append({"kind": "cavity", "grid": int(round(np.sqrt(N / 2.0))) + 1, "re": r,
-                      "tau": tau_from_re(r, rule=tau_rule), "flux": flux, "seed": seed * 100_003 + i,
+        g = int(round(np.sqrt(N / 2.0))) + 1
+        sc = cavity_lattice_scale(g) if units == "lattice" else 1.0
+        specs.append({"kind": "cavity", "grid": g, "re": r, "scale": sc,
+                      "tau": tau_from_re(r, length=sc, rule=tau_rule), "flux": flux, "seed": seed * 100_003 + i,
                       "fv_dt": fv_dt})
     for i in range(n_porous):
         N = int(rng.uniform(*porous_cells))
         k = int(rng.integers(obstacles[0], obstacles[1] + 1))
         r = float(rng.uniform(*re))
-        specs.append({"kind": "porous", "obstacles": k, "n_target": N, "re": r,
-                      "tau": tau_from_re(r, rule=tau_rule),
+        sc = porous_lattice_scale(N, porosity) if units == "lattice" else 1.0
+        specs.append({"kind": "porous", "obstacles": k, "n_target": N, "re": r, "scale": sc,
+                      "tau": tau_from_re(r, length=sc, rule=tau_rule),
                       "porosity": porosity, "flux": flux, "seed": seed * 100_003 + n_cavity + i,
                       "fv_dt": fv_dt, "rho_in": rho_in, "rho_out": rho_out})
     if n_ranks > 1:
@@ -165,7 +191,7 @@ def batch_suite(seed: int = 0, n_cavity: int = 128, n_porous: int = 128, flux: s
         cases = [_make(s) for s in specs]
     desc = []
     for s, cs in zip(specs, cases):
-        d = {k: v for k, v in s.items() if k in ("kind", "grid", "obstacles", "re", "tau")}
+        d = {k: v for k, v in s.items() if k in ("kind", "grid", "obstacles", "re", "tau", "scale")}
         d["cells"] = int(cs[1].pdf.shape[0])
         d["dt"] = float(cs[0].delta_t)
         desc.append(d)
