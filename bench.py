@@ -69,8 +69,9 @@ def parse():
                          "tau = 3UL/Re + 1/2) or the unit square (finite-volume update, tau = 3UL/Re)")
     ap.add_argument("--threshold", type=float, default=1e-6)
     ap.add_argument("--check-every", type=int, default=100)
-    ap.add_argument("--check-time", type=float, default=5.0,
-                    help="batch: each case's residual window in its own time units")
+    ap.add_argument("--check-time", type=float, default=None,
+                    help="residual window in each case's own time units (default: 100 for the batch in "
+                         "lattice units, 5 otherwise)")
     ap.add_argument("--step-cap", type=int, default=None,
                     help="per-case step cap (default: 20000 for batch, 100000 for warmstart)")
     # --workload warmstart: learned warm start against the uniform start
@@ -618,7 +619,8 @@ def run_batch(args):
     cells = np.array([d["cells"] for d in desc], np.int64)
     thr, every, cap = args.threshold, args.check_every, args.step_cap or 1_000_000
     # per-case window in whole chunks, as the batch loop takes it
-    window = np.array([int(np.ceil(max(1, int(np.ceil(args.check_time / d["dt"]))) / every)) * every
+    ct = args.check_time if args.check_time is not None else (100.0 if lattice else 5.0)
+    window = np.array([int(np.ceil(max(1, int(np.ceil(ct / d["dt"]))) / every)) * every
                        for d in desc], np.int64)
 
     b = Batch([(c, f, n) for _, c, f, n in suite], device=local, finite_volume=fv)
@@ -628,7 +630,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     barrier(ws)
     t = time.perf_counter()
-    steps_b, res_b, st_b = b.run_to_steady(thr, every, cap, check_time=args.check_time)
+    steps_b, res_b, st_b = b.run_to_steady(thr, every, cap, check_time=ct)
     b.sync()
     batched_s = max_over_ranks(time.perf_counter() - t, ws, local)
     b.close()
@@ -667,6 +669,13 @@ def run_batch(args):
             "steps_median_porous": int(np.median(steps_b[kinds == "porous"])) if (kinds == "porous").any() else None,
             "res_max_converged": float(res_b[st_b == 1].max()) if (st_b == 1).any() else None,
             "converged_at_exact_fixed_point": int(np.sum((st_b == 1) & (res_b == 0.0))),
+            "status_by_kind": {k: {name: int(np.sum((kinds == k) & (st_b == code)))
+                                   for name, code in (("converged", 1), ("capped", 0), ("nonfinite", 2),
+                                                      ("frozen", 3), ("stalled", 4))}
+                               for k in ("cavity", "porous")},
+            "stalled_cases": [{"kind": str(kinds[i]), "cells": int(cells[i]), "re": round(float(desc[i]["re"]), 1),
+                               "tau": round(float(desc[i]["tau"]), 4), "steps": int(steps_b[i]),
+                               "res": float(res_b[i])} for i in np.nonzero(st_b == 4)[0]],
             "n_gpus": ws, "scaling": "strong", "dtype": "f32", "data": "synthetic",
             "autotune": tune,
             "config": {"workload": f"{args.cases} independent cases: {n_cav} lid cavities (2k-60k cells, lid 0.1), "
@@ -677,7 +686,7 @@ def run_batch(args):
                                        "unit square, tau = 3UL/Re, finite-volume update, "
                                        "dt = min(area/perimeter, tau)"),
                        "units": args.units, "cells": int(all_cells), "flux": args.flux,
-                       "check_every": every, "check_time": args.check_time, "step_cap": cap,
+                       "check_every": every, "check_time": ct, "step_cap": cap,
                        "setup_s": round(setup_s, 1)}}
     print(json.dumps(line), flush=True)
 
@@ -685,8 +694,8 @@ def run_batch(args):
 def _ws_case(spec):
     from fvdbm_jax_gb300 import cases as CS
     return CS.porous_square(spec["obstacles"], spec["n_target"], spec["tau"], rho_in=spec["rho_in"],
-                            rho_out=spec["rho_out"], porosity=spec["porosity"], fv_dt=1.0,
-                            seed=spec["seed"], mesher=True)
+                            rho_out=spec["rho_out"], porosity=spec["porosity"], fv_dt=spec["fv_dt"],
+                            seed=spec["seed"], mesher=True, scale=spec["scale"])
 
 
 def _ws_sample(job):
@@ -706,10 +715,13 @@ def run_warmstart(args):
     both as one Batch with the same loop; and the plain solver runs each case
     alone from the uniform start.  Reports steps and seconds.
 
-    Regime: the finite-volume scaled update, tau = 0.003 (Re 100 with
-    U = 0.1, L = 1 by nu = c_s^2 tau), dt = min(area / perimeter, tau),
-    inlet density 1.01-1.05, outlet 0.95-0.99; residual windows of
-    ``--check-time`` time units per case."""
+    Regime (``--units lattice``, the default): the mesh spacing about 1,
+    the reference's update, tau = 3 U L / Re + 1/2 with Re 100, U = 0.1 and L
+    the side in cells, dt = 0.5 min edge.  ``--units unit``: the unit square,
+    the finite-volume scaled update, tau = 0.003 (Re 100 with U = 0.1, L = 1
+    by nu = c_s^2 tau), dt = min(area / perimeter, tau).  Inlet density
+    1.01-1.05, outlet 0.95-0.99; residual windows of ``--check-time`` time
+    units per case (default 100 in lattice units, else 5)."""
     import concurrent.futures as cf
     import multiprocessing as mp
 
@@ -722,10 +734,19 @@ def run_warmstart(args):
     rng = np.random.default_rng(2024)
     lo_cells, hi_cells = (int(v) for v in args.ws_cells.split(","))
 
+    from fvdbm_jax_gb300 import cases as CS
+    lattice = args.units == "lattice"
+    fv = not lattice
+
     def spec(i):
-        return {"obstacles": int(rng.integers(20, 201)), "n_target": int(rng.uniform(lo_cells, hi_cells)),
-                "tau": 0.003, "rho_in": float(rng.uniform(1.01, 1.05)), "rho_out": float(rng.uniform(0.95, 0.99)),
-                "porosity": float(rng.uniform(0.75, 0.85)), "seed": 50_000 + i}
+        s = {"obstacles": int(rng.integers(20, 201)), "n_target": int(rng.uniform(lo_cells, hi_cells)),
+             "tau": 0.003, "rho_in": float(rng.uniform(1.01, 1.05)), "rho_out": float(rng.uniform(0.95, 0.99)),
+             "porosity": float(rng.uniform(0.75, 0.85)), "seed": 50_000 + i, "scale": 1.0, "fv_dt": 1.0}
+        if lattice:
+            s["scale"] = CS.porous_lattice_scale(s["n_target"], s["porosity"])
+            s["tau"] = CS.tau_from_re(100.0, length=s["scale"], rule="notebook")
+            s["fv_dt"] = None
+        return s
     specs = [spec(i) for i in range(args.train_cases + args.eval_cases)]
     t0 = time.perf_counter()
     # one pool of host workers, started before the first GPU call, builds the
@@ -736,11 +757,11 @@ def run_warmstart(args):
     train, evalc = allc[:args.train_cases], allc[args.train_cases:]
     tspec, espec = specs[:args.train_cases], specs[args.train_cases:]
     thr, every, cap = args.threshold, args.check_every, args.step_cap or 1_000_000
-    ct = args.check_time
+    ct = args.check_time if args.check_time is not None else (100.0 if lattice else 5.0)
 
     # training data: the solver's own steady states
     t = time.perf_counter()
-    b = Batch([c[1:4] for c in train], finite_volume=True)
+    b = Batch([c[1:4] for c in train], finite_volume=fv)
     b.init()
     steps_t, res_t, st_t = b.run_to_steady(thr, every, cap, check_time=ct)
     state = b.state()
@@ -767,7 +788,7 @@ def run_warmstart(args):
 
     # held-out: uniform start against the predicted start
     def timed(init):
-        bb = Batch([c[1:4] for c in evalc], finite_volume=True)
+        bb = Batch([c[1:4] for c in evalc], finite_volume=fv)
         bb.init()
         bb.sync()
         t1 = time.perf_counter()
@@ -799,7 +820,7 @@ def run_warmstart(args):
     from fvdbm_jax_gb300 import Environment
     seq_s, seq_steps = 0.0, 0
     for case in evalc:
-        env = Environment(*case[1:4], finite_volume=True)
+        env = Environment(*case[1:4], finite_volume=fv)
         env.init()
         env.sync()
         w = int(np.ceil(max(1, int(np.ceil(ct / float(case[0].delta_t)))) / every)) * every
@@ -841,10 +862,13 @@ def run_warmstart(args):
             "n_gpus": 1, "dtype": "f32 solver; bf16 weights / f32 accumulate network (TF32 tensor cores)",
             "data": "synthetic",
             "config": {"workload": f"porous squares, 20-200 obstacles, porosity 0.75-0.85, {lo_cells}-{hi_cells} "
-                                   f"cells, rho_in 1.01-1.05 / rho_out 0.95-0.99, tau 0.003 (Re 100), "
-                                   f"finite-volume update, dt = min(area/perimeter, tau), upwind; "
-                                   f"{args.train_cases} training + {args.eval_cases} held-out geometries",
-                       "check_every": every, "check_time": ct, "step_cap": cap, "setup_s": round(setup_s, 1)}}
+                                   f"cells, rho_in 1.01-1.05 / rho_out 0.95-0.99, Re 100, " + (
+                                       "lattice units (mesh spacing ~1), tau = 3UL/Re + 1/2 with L the side in "
+                                       "cells, the reference's update, dt = 0.5 min edge" if lattice else
+                                       "unit square, tau 0.003, finite-volume update, dt = min(area/perimeter, tau)")
+                                   + f", upwind; {args.train_cases} training + {args.eval_cases} held-out geometries",
+                       "units": args.units, "check_every": every, "check_time": ct, "step_cap": cap,
+                       "setup_s": round(setup_s, 1)}}
     print(json.dumps(line), flush=True)
 
 
