@@ -28,3 +28,24 @@ def test_rank_subsets_match_the_full_suite():
                                    porous_cells=(3000, 5000), obstacles=(5, 10), rank=r, n_ranks=2)
         seen += [key(d) for d in dsub]
     assert sorted(seen) == sorted(key(d) for d in dfull)
+
+
+def test_lattice_unit_scales_give_unit_spacing():
+    """Cases meshed in lattice units have a mesh spacing of about 1, and
+    their tau follows the notebooks' rule with L the side in cells."""
+    from fvdbm_jax_gb300 import cases as CS
+    import numpy as np
+    sc = CS.cavity_lattice_scale(21)
+    dyn, c, f, n, m = CS.lid_cavity(21, 0.6, scale=sc, mesher=True)
+    L = np.asarray(m.face_lengths)
+    assert sc == 20.0 and 0.8 < np.median(L) < 1.2
+    assert abs(float(dyn.delta_t) - 0.5 * L.min()) < 1e-6
+    sp = CS.porous_lattice_scale(6000, 0.8)
+    dyn, c, f, n, m = CS.porous_square(20, 6000, 0.6, porosity=0.8, scale=sp, mesher=True, seed=3)
+    L = np.asarray(m.face_lengths)
+    assert 0.7 < np.median(L) < 1.3, np.median(L)
+    suite, desc = CS.batch_suite(seed=1, n_cavity=2, n_porous=1, cavity_cells=(2000, 3000),
+                                 porous_cells=(6000, 7000), obstacles=(20, 30), units="lattice")
+    for d in desc:
+        assert d["scale"] > 10
+        assert abs(d["tau"] - (3 * CS.LID_U * d["scale"] / d["re"] + 0.5)) < 1e-12

@@ -81,3 +81,33 @@ def test_frozen_and_nonfinite_statuses():
     with pytest.raises(nat.NonFiniteError):
         env.run_to_steady(1e-6, 20, 200)
     env.close()
+
+
+def test_lattice_units_reach_the_threshold():
+    """In lattice units (mesh spacing ~1, the reference's update, the
+    notebooks' tau rule, dt = 0.5 min edge) cavities and a porous square
+    converge below 1e-6: genuine convergence, not a frozen float32 state;
+    each case alone stops at the same step."""
+    from fvdbm_jax_gb300 import Batch, Environment
+    from fvdbm_jax_gb300 import cases as CS
+    cases = []
+    for n_, re in ((21, 100.0), (31, 400.0)):
+        sc = CS.cavity_lattice_scale(n_)
+        cases.append(CS.lid_cavity(n_, CS.tau_from_re(re, length=sc), seed=n_, scale=sc))
+    sp = CS.porous_lattice_scale(4000, 0.8)
+    cases.append(CS.porous_square(10, 4000, CS.tau_from_re(200.0, length=sp), porosity=0.8, rho_in=1.05,
+                                  rho_out=0.95, seed=5, scale=sp))
+    every, T, thr, cap = 100, 100.0, 1e-6, 200_000
+    b = Batch([(c, f, n) for _, c, f, n in cases])
+    b.init()
+    steps, res, status = b.run_to_steady(thr, every, cap, check_time=T)
+    b.close()
+    assert list(status) == [1, 1, 1], (status, res, steps)
+    assert np.all((res > 0) & (res < thr)), res
+    for s, (dyn, c, f, n) in enumerate(cases):
+        window = int(np.ceil(max(1, int(np.ceil(T / float(dyn.delta_t)))) / every)) * every
+        env = Environment(c, f, n)
+        env.init()
+        k, r = env.run_to_steady(thr, window, cap)
+        env.close()
+        assert k == steps[s] and 0 < r < thr, (s, k, steps[s], r)
