@@ -418,10 +418,14 @@ __device__ __forceinline__ void fused_cell(const DevPlan& p, const float* __rest
 
 // ---------------------------------------------------------------------------
 // The fast family's cell update (FVDBM_KERNEL_FAST): the same step with
-// contracted arithmetic (fvdbm_math.cuh, "contracted forms").  Direction q = 0
-// has xi.n = 0 and carries no flux; the pairs (1, 3), (2, 4), (5, 7), (6, 8)
-// share |xi.n|, so one comparison picks both upwind sides (at xi.n = 0 the
-// choice does not matter: the flux is zero either way).
+// contracted arithmetic (fvdbm_math.cuh, "contracted forms") on compact face
+// slots: a = n * (L*sigma [*scale] [/area]) per face slot (HfFastRows), so
+// that xi_q . a is the flux coefficient of direction q.  Direction q = 0 has
+// xi.n = 0 and carries no flux; the pairs (1, 3), (2, 4), (5, 7), (6, 8)
+// share |xi.a|.
+//
+// All nine pdfs across face slot `code` (Lax-Wendroff): the neighbour's, or
+// the ghost value m + (m - f) * rg as a multiply-add.
 __device__ __forceinline__ void face_other_fast(const DevPlan& p, const float* __restrict__ fin, int code,
                                                 const float f[Q], float o[Q]) {
   const int other = code >> HF_SHIFT;
@@ -438,30 +442,20 @@ __device__ __forceinline__ void face_other_fast(const DevPlan& p, const float* _
   }
 }
 
-// Flux of one face slot from the compact slot: a = n * (L*sigma [*scale]
-// [/area]) per face slot (HfFastRows), so that xi_q . a is the flux
-// coefficient of direction q and its sign picks the upwind side.
-template <int SCHEME>
-__device__ __forceinline__ void face_flux_fast(int code, float ax, float ay, float r, float g, const float f[Q],
-                                               const float o[Q], float acc[Q]) {
+// Lax-Wendroff flux of one compact face slot:
+// phi = l + (r - l) * (d0/(d0+d1) - (xi.n) dt/(2(d0+d1))), where
+// (xi.n) dt/(2(d0+d1)) = (xi.a) * g.
+__device__ __forceinline__ void face_lw_fast(int code, float ax, float ay, float r, float g, const float f[Q],
+                                             const float o[Q], float acc[Q]) {
   const bool slot1 = (code & HF_SLOT1) != 0;
   const float a4[4] = {ax, ay, ax + ay, ay - ax};
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int qp = j < 2 ? 1 + j : 5 + (j - 2), qm = qp + 2;  // xi.a = +a4[j], -a4[j]
-    float pp, pm;
-    if (SCHEME == 0) {
-      const bool up = (a4[j] >= 0.0f) != slot1;
-      pp = up ? f[qp] : o[qp];
-      pm = up ? o[qm] : f[qm];
-    } else {
-      // Lax-Wendroff: phi = l + (r - l) * (d0/(d0+d1) - (xi.n) dt/(2(d0+d1))),
-      // (xi.n) dt/(2(d0+d1)) = (xi.a) * g
-      const float lp = slot1 ? o[qp] : f[qp], rp = slot1 ? f[qp] : o[qp];
-      const float lm = slot1 ? o[qm] : f[qm], rm = slot1 ? f[qm] : o[qm];
-      pp = __fmaf_rn(rp - lp, __fmaf_rn(-a4[j], g, r), lp);
-      pm = __fmaf_rn(rm - lm, __fmaf_rn(a4[j], g, r), lm);
-    }
+    const float lp = slot1 ? o[qp] : f[qp], rp = slot1 ? f[qp] : o[qp];
+    const float lm = slot1 ? o[qm] : f[qm], rm = slot1 ? f[qm] : o[qm];
+    const float pp = __fmaf_rn(rp - lp, __fmaf_rn(-a4[j], g, r), lp);
+    const float pm = __fmaf_rn(rm - lm, __fmaf_rn(a4[j], g, r), lm);
     acc[qp] = __fmaf_rn(pp, a4[j], acc[qp]);
     acc[qm] = __fmaf_rn(-pm, a4[j], acc[qm]);
   }
@@ -545,7 +539,7 @@ __device__ __forceinline__ void fused_cell_fast(const DevPlan& p, const float* _
       face_other_fast(p, fin, code[k], f, o);
       const float r = __uint_as_float(__ldg(hb + HX.r(k) * 32));
       const float g = __uint_as_float(__ldg(hb + HX.g(k) * 32));
-      face_flux_fast<SCHEME>(code[k], ax[k], ay[k], r, g, f, o, acc);
+      face_lw_fast(code[k], ax[k], ay[k], r, g, f, o, acc);
     }
   }
   float rho, ux, uy, eq[Q];
