@@ -77,6 +77,9 @@ def parse():
     # --workload warmstart: learned warm start against the uniform start
     ap.add_argument("--train-cases", type=int, default=400)
     ap.add_argument("--eval-cases", type=int, default=64)
+    ap.add_argument("--group-cases", type=int, default=200,
+                    help="warmstart: training cases meshed, solved and turned into samples per group "
+                         "(bounds the host memory the cases take)")
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--ws-cells", type=str, default="50000,200000",
                     help="warmstart: cell-count range of the porous geometries")
@@ -752,33 +755,47 @@ def run_warmstart(args):
     # one pool of host workers, started before the first GPU call, builds the
     # cases and later the per-case network inputs
     ex = cf.ProcessPoolExecutor(min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn"))
-    allc = list(ex.map(_ws_case, specs, chunksize=2))
-    setup_s = time.perf_counter() - t0
-    train, evalc = allc[:args.train_cases], allc[args.train_cases:]
     tspec, espec = specs[:args.train_cases], specs[args.train_cases:]
+    evalc = list(ex.map(_ws_case, espec, chunksize=2))
+    setup_s = time.perf_counter() - t0
     thr, every, cap = args.threshold, args.check_every, args.step_cap or 1_000_000
     ct = args.check_time if args.check_time is not None else (100.0 if lattice else 5.0)
 
-    # training data: the solver's own steady states
-    t = time.perf_counter()
-    b = Batch([c[1:4] for c in train], finite_volume=fv)
-    b.init()
-    steps_t, res_t, st_t = b.run_to_steady(thr, every, cap, check_time=ct)
-    state = b.state()
-    data_s = time.perf_counter() - t
-    # converged and frozen states alike: an update below half an ulp rounds
-    # away, so either way the float32 iteration has stopped inside a band
-    # around the discrete steady state whose width grows like 1/dt
-    jobs = []
-    for s, (case, sp) in enumerate(zip(train, tspec)):
-        if st_t[s] not in (1, 3):
-            continue
-        rho, vel = WS.macros(b.case_state(s, state)["pdf"])
-        jobs.append((case, sp["rho_in"], sp["rho_out"], rho, vel))
-    b.close()
-    del state
-    samples = list(ex.map(_ws_sample, jobs, chunksize=2))
-    WS.solve_potentials(samples)
+    # training data: the solver's own steady states, a group of cases at a
+    # time (meshed by the workers, solved as one batch, turned into samples;
+    # only the samples are kept)
+    data_s, samples, steps_t, st_t, train_cells = 0.0, [], [], [], 0
+    G = max(1, args.group_cases)
+    for g0 in range(0, len(tspec), G):
+        gspec = tspec[g0:g0 + G]
+        t = time.perf_counter()
+        train = list(ex.map(_ws_case, gspec, chunksize=2))
+        setup_s += time.perf_counter() - t
+        t = time.perf_counter()
+        b = Batch([c[1:4] for c in train], finite_volume=fv)
+        b.init()
+        stp, _, sts = b.run_to_steady(thr, every, cap, check_time=ct)
+        state = b.state()
+        data_s += time.perf_counter() - t
+        steps_t += list(stp)
+        st_t += list(sts)
+        # converged and frozen states alike: an update below half an ulp
+        # rounds away, so either way the float32 iteration has stopped inside
+        # a band around the discrete steady state whose width grows like 1/dt
+        jobs = []
+        for s, (case, sp) in enumerate(zip(train, gspec)):
+            train_cells += int(case[1].pdf.shape[0])
+            if sts[s] not in (1, 3):
+                continue
+            rho, vel = WS.macros(b.case_state(s, state)["pdf"])
+            jobs.append((case, sp["rho_in"], sp["rho_out"], rho, vel))
+        b.close()
+        del state, train
+        grp = list(ex.map(_ws_sample, jobs, chunksize=2))
+        del jobs
+        WS.solve_potentials(grp)
+        samples += grp
+    steps_t, st_t = np.array(steps_t), np.array(st_t)
     t = time.perf_counter()
     net = WS.MPNN(seed=0)
     hist = net.fit(samples, epochs=args.epochs, lr=3e-3, log_every=max(args.epochs // 10, 1),
