@@ -60,8 +60,10 @@ def parse():
     ap.add_argument("--no-above-l2", action="store_true",
                     help="skip the ~4M-triangle point whose per-step traffic is well above L2")
     ap.add_argument("--e2e-steps", type=int, default=100)
-    ap.add_argument("--kernel", default="fast",
-                    choices=["auto", "one", "fused", "fused_nodes", "fast", "persist", "staged", "tile", "tile_split"])
+    ap.add_argument("--kernel", default=None,
+                    choices=["auto", "one", "fused", "fused_nodes", "fast", "persist", "staged", "tile", "tile_split"],
+                    help="kernel family timed (default: fast for the porous workloads, auto otherwise: on "
+                         "the small cavity and channel meshes the two-launch family is the faster one)")
     # --workload batch: time-to-steady of many independent cases, batched vs one at a time
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--units", default="lattice", choices=["lattice", "unit"],
@@ -87,7 +89,10 @@ def parse():
                     help="warmstart: cells per training minibatch")
     ap.add_argument("--graph-cells", type=int, default=1_500_000,
                     help="mpnn_epoch: cells of the synthetic graph")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.kernel is None:
+        args.kernel = "fast" if args.workload.startswith("porous") else "auto"
+    return args
 
 
 def workload(name, flux, seed):
