@@ -249,7 +249,7 @@ def solve_potentials(samples, device: int = 0, rtol: float = 1e-6, max_iter: int
     one block-diagonal system (``fvdbm_pcg``: Jacobi-preconditioned
     conjugate gradients, float32 vectors, float64 fixed-order dot products),
     then each gradient is formed on the host.  Returns (iterations, relative
-    residual)."""
+    residual); a residual above rtol means that max_iter ran out first."""
     import ctypes as C
 
     import torch
