@@ -11,8 +11,8 @@ oracle (the reference step restated in C, float32, no contraction):
   dt = 0.5 * min edge, leaves 99 % of the cells unchanged in float32 over
   such a horizon).  The test asserts that the velocity field moves.
 
-Every comparison uses ``np.array_equal``: the benchmark spec's 1e-5 relative
-tolerance is met with zero difference."""
+Every comparison uses ``np.array_equal``: a 1e-5 relative tolerance on rho
+and u is met with zero difference."""
 import numpy as np
 import pytest
 

@@ -50,3 +50,49 @@ def test_chunk_tables_cover_each_row_in_order():
             for e in range(cst[k], cst[k + 1]):
                 got[r, c[e]] += w[e]
     assert np.allclose(got, want)
+
+
+def test_potential_system_and_deferred_sample():
+    """The potential-flow estimate as a linear problem: A is symmetric with
+    a positive, dominant diagonal; the host solve satisfies it; the affine
+    gradient map equals the Green-Gauss sum over face values written out
+    directly; a deferred sample leaves the three columns for the GPU solve."""
+    import scipy.sparse.linalg as spl
+    from fvdbm_jax_gb300 import cases
+    from fvdbm_jax_gb300 import warmstart as WS
+    dyn, c, f, n, m = cases.porous_square(10, 2500, 0.65, rho_in=1.02, rho_out=0.98, porosity=0.8,
+                                          delta_t=1.0, seed=9, mesher=True)
+    ps = WS.potential_system(m, c, f, n, 1.02, 0.98)
+    A = ps.A
+    assert abs(A - A.T).max() == 0.0
+    d = A.diagonal()
+    off = np.asarray(abs(A).sum(1)).reshape(-1) - np.abs(d)
+    assert np.all(d > 0) and np.all(d >= off - 1e-12 * d)
+    phi = spl.spsolve(A.tocsc(), ps.rhs)
+    assert np.abs(A @ phi - ps.rhs).max() <= 1e-10 * max(np.abs(ps.rhs).max(), 1.0)
+    p2, gx, gy = WS.potential(m, c, f, n, 1.02, 0.98)
+    assert np.allclose(p2, phi, rtol=0, atol=1e-12)
+    # Green-Gauss written out: face values, then sum_k sign_k pf n L / area
+    fc = np.asarray(f.stencil_cells_index, np.int64)
+    sd = np.asarray(f.stencil_dists, np.float64)
+    L = np.asarray(f.L, np.float64).reshape(-1)
+    fn = np.asarray(f.nodes_index, np.int64)
+    t = np.asarray(n.type).reshape(-1)
+    nr = np.asarray(n.rho, np.float64).reshape(-1)
+    inner = (fc[:, 0] >= 0) & (fc[:, 1] >= 0)
+    open_ = ~inner & (t[fn[:, 0]] == 2) & (t[fn[:, 1]] == 2)
+    owner = np.where(fc[:, 0] >= 0, fc[:, 0], fc[:, 1])
+    pf = phi[owner].copy()
+    a, b = fc[inner, 0], fc[inner, 1]
+    pf[inner] = (phi[a] * sd[inner, 1] + phi[b] * sd[inner, 0]) / (sd[inner, 0] + sd[inner, 1])
+    pf[open_] = 0.5 * ((nr[fn[open_, 0]] - 0.98) + (nr[fn[open_, 1]] - 0.98)) / 0.04
+    cf = np.asarray(c.face_indices, np.int64)
+    cs = np.asarray(c.face_normals, np.float64)
+    nn = np.asarray(f.n, np.float64)
+    g = (cs[:, :, None] * (pf[cf] * L[cf])[:, :, None] * nn[cf]).sum(1) / np.asarray(m.cell_areas).reshape(-1, 1)
+    assert np.allclose(gx, g[:, 0], rtol=1e-10, atol=1e-12) and np.allclose(gy, g[:, 1], rtol=1e-10, atol=1e-12)
+    s = WS.sample((dyn, c, f, n, m), 1.02, 0.98, defer_potential=True)
+    assert s.pending is not None and s.pending.n == s.n
+    assert not s.x[:, 6:].any()
+    full = WS.sample((dyn, c, f, n, m), 1.02, 0.98)
+    assert full.pending is None and np.array_equal(full.x[:, :6], s.x[:, :6])
