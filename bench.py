@@ -373,8 +373,10 @@ def bitexact_point(args, local, flush_l2, c, f, n, K, desc):
     peak, peak_kind = measured_peaks()
     N, B = info["n_cells"], info["bytes_per_step"]
     env.close()
-    assert info["launches_per_step"] == 1
-    return {"kernel": {7: "k_fused_nodes"}.get(info["kernel"], str(info["kernel"])),
+    # the whole step: one launch for the single-launch family (meshes of 2^18
+    # cells or more), else the two-launch family's pair
+    return {"kernel": {7: "k_fused_nodes", 2: "k_nodes_cp + k_fused"}.get(info["kernel"], str(info["kernel"])),
+            "launches_per_step": info["launches_per_step"],
             "note": "bit for bit with the reference's step; the same flushed protocol",
             "avg_launch_us": round(us, 3), "mcups": round(N / us, 1),
             "frac": round(B / us / 1e3 / peak, 4), "traffic": profiled_traffic("k_fused_nodes", desc), "steps": K}
