@@ -65,7 +65,9 @@ EXPORTS = ["fvdbm_create", "fvdbm_set_state", "fvdbm_step", "fvdbm_step_phase", 
            "fvdbm_batch_run_to_steady_time", "fvdbm_batch_residual_cases",
            "fvdbm_mp_dense_fwd", "fvdbm_mp_dense_bwd_data", "fvdbm_mp_wgrad_scratch", "fvdbm_mp_dense_bwd_weight",
            "fvdbm_mp_relu_bwd", "fvdbm_mp_spmm", "fvdbm_mp_mse_scratch", "fvdbm_mp_mse", "fvdbm_mp_adam",
-           "fvdbm_mp_to_bf16", "fvdbm_mp_spmm_chunked", "fvdbm_pcg_work_bytes", "fvdbm_pcg"]
+           "fvdbm_mp_to_bf16", "fvdbm_mp_spmm_chunked", "fvdbm_pcg_work_bytes", "fvdbm_pcg",
+           "fvdbm_ws_wall_distance", "fvdbm_ws_potential_rows", "fvdbm_ws_potential_grad", "fvdbm_ws_mesh_mean",
+           "fvdbm_ws_bin_ids", "fvdbm_ws_bin_rows"]
 
 
 def lib_path() -> str:
@@ -119,6 +121,13 @@ def lib(build_if_missing: bool = True) -> C.CDLL:
     L.fvdbm_pcg_work_bytes.restype = sz
     L.fvdbm_pcg.argtypes = [i32, u64, u64, u64, u64, u64, i32, C.c_double, i32, u64, sz, u64,
                             C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    L.fvdbm_ws_wall_distance.argtypes = [i32, u64, u64, i32, u64, u64, u64, u64]
+    L.fvdbm_ws_potential_rows.argtypes = [i32, u64, u64, u64, u64, u64, u64, i32, u64, u64, u64, u64]
+    L.fvdbm_ws_potential_grad.argtypes = [i32, u64, u64, u64, u64, u64, u64, u64, u64, u64, u64, u64, u64, u64]
+    L.fvdbm_ws_mesh_mean.argtypes = [i32, u64, u64, i32, u64, u64, u64]
+    dbl = C.c_double
+    L.fvdbm_ws_bin_ids.argtypes = [i32, u64, dbl, dbl, dbl, dbl, i32, u64, u64, u64]
+    L.fvdbm_ws_bin_rows.argtypes = [i32, i32, u64, u64, u64, i32, i32, u64, u64, u64, u64]
     L.fvdbm_run_to_steady.argtypes = [vp, C.c_double, C.c_int32, C.c_int64, C.POINTER(C.c_int64),
                                       C.POINTER(C.c_double)]
     L.fvdbm_get_cells.argtypes = [vp, _f32p, _f32p, _f32p, _f32p]

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I" + os.path.join(ROOT, "include")]
 SOURCES = ["kernels.cu", "tile.cu", "monitor.cu", "capi.cu", "plan.cpp", "batch.cpp", "mpnn.cu", "d2q13.cu",
-           "pcg.cu"]
+           "pcg.cu", "features.cu"]
 HEADERS = [os.path.join(CSRC, "fvdbm_internal.h"), os.path.join(CSRC, "fvdbm_math.cuh"),
            os.path.join(ROOT, "include", "fvdbm.h"), os.path.join(ROOT, "include", "fvdbm_mpnn.h")]
 

@@ -3,9 +3,11 @@
 // (all held-out cases together as one block-diagonal system).  No
 // counterpart in the reference.
 //
-// Vectors are float32; every dot product is summed in double over fixed
-// per-block ranges, then over the blocks in block order by one block, so an
-// iteration is bitwise reproducible.  The scalars of the recurrence (alpha,
+// Vectors are float32.  Every dot product is summed by each thread in
+// float32 (multiply-adds; the rows of a thread are few) and then in double
+// over the block and over the blocks in block order by one block, so an
+// iteration is bitwise reproducible (float64 arithmetic is slow on this GPU,
+// so it is kept to the reductions).  The scalars of the recurrence (alpha,
 // beta, r.z) stay on the device; the host reads ||r||^2 every check_every
 // iterations to stop.
 //
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(PT) k_init(int n, const int* __restrict__ ip, 
                                             const float* __restrict__ x, float* __restrict__ dinv,
                                             float* __restrict__ r, float* __restrict__ z, float* __restrict__ p,
                                             double* __restrict__ part) {
-  double acc[3] = {0.0, 0.0, 0.0};
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
   for (int i = blockIdx.x * PT + threadIdx.x; i < n; i += gridDim.x * PT) {
     float d = 0.0f;
     for (int e = ip[i]; e < ip[i + 1]; ++e)
@@ -83,10 +85,11 @@ __global__ void __launch_bounds__(PT) k_init(int n, const int* __restrict__ ip, 
     r[i] = ri;
     z[i] = zi;
     p[i] = zi;
-    acc[0] += double(ri) * double(zi);
-    acc[1] += double(ri) * double(ri);
-    acc[2] += double(b[i]) * double(b[i]);
+    a0 = __fmaf_rn(ri, zi, a0);
+    a1 = __fmaf_rn(ri, ri, a1);
+    a2 = __fmaf_rn(b[i], b[i], a2);
   }
+  double acc[3] = {a0, a1, a2};
   block_sum_store<3>(acc, part + size_t(blockIdx.x) * 3);
 }
 
@@ -94,12 +97,13 @@ __global__ void __launch_bounds__(PT) k_init(int n, const int* __restrict__ ip, 
 __global__ void __launch_bounds__(PT) k_spmv(int n, const int* __restrict__ ip, const int* __restrict__ ix,
                                             const float* __restrict__ v, const float* __restrict__ p,
                                             float* __restrict__ q, double* __restrict__ part) {
-  double acc[1] = {0.0};
+  float a0 = 0.0f;
   for (int i = blockIdx.x * PT + threadIdx.x; i < n; i += gridDim.x * PT) {
     const float qi = row_dot(n, ip, ix, v, p, i);
     q[i] = qi;
-    acc[0] += double(p[i]) * double(qi);
+    a0 = __fmaf_rn(p[i], qi, a0);
   }
+  double acc[1] = {a0};
   block_sum_store<1>(acc, part + size_t(blockIdx.x) * 3);
 }
 
@@ -136,16 +140,17 @@ __global__ void __launch_bounds__(PT) k_update(int n, const double* __restrict__
                                               float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
                                               double* __restrict__ part) {
   const float a = float(s[S_ALPHA]);
-  double acc[3] = {0.0, 0.0, 0.0};
+  float a0 = 0.0f, a1 = 0.0f;
   for (int i = blockIdx.x * PT + threadIdx.x; i < n; i += gridDim.x * PT) {
     x[i] = __fmaf_rn(a, p[i], x[i]);
     const float ri = __fmaf_rn(-a, q[i], r[i]);
     const float zi = ri * dinv[i];
     r[i] = ri;
     z[i] = zi;
-    acc[0] += double(ri) * double(zi);
-    acc[1] += double(ri) * double(ri);
+    a0 = __fmaf_rn(ri, zi, a0);
+    a1 = __fmaf_rn(ri, ri, a1);
   }
+  double acc[3] = {a0, a1, 0.0};
   block_sum_store<3>(acc, part + size_t(blockIdx.x) * 3);
 }
 

@@ -247,7 +247,7 @@ def solve_potentials(samples, device: int = 0, rtol: float = 1e-6, max_iter: int
     """Fill the potential-flow columns of the samples built with
     ``defer_potential=True``: their systems are solved together on the GPU as
     one block-diagonal system (``fvdbm_pcg``: Jacobi-preconditioned
-    conjugate gradients, float32 vectors, float64 fixed-order dot products),
+    conjugate gradients, float32 vectors, fixed-order dot products),
     then each gradient is formed on the host.  Returns (iterations, relative
     residual); a residual above rtol means that max_iter ran out first."""
     import ctypes as C
@@ -707,6 +707,194 @@ def sample(case, rho_in: float, rho_out: float, rho=None, vel=None, scales=SCALE
         x = features(m, c, f, n, rho_in, rho_out)
     t = None if rho is None else targets(rho, vel, rho_in, rho_out)
     return Sample(x, aggregations(f, m.cell_centers, x.shape[0], scales), t, pending=pend)
+
+
+def _case_arrays(case, rho_in: float, rho_out: float):
+    """Host arrays of one case for the GPU feature kernels, index ranges
+    checked (the kernels trust them)."""
+    dyn, c, f, n, m = case
+    cf = np.ascontiguousarray(np.asarray(c.face_indices), np.int32)
+    cs = np.ascontiguousarray(np.asarray(c.face_normals), np.float32)
+    fc = np.ascontiguousarray(np.asarray(f.stencil_cells_index), np.int32)
+    fd = np.ascontiguousarray(np.asarray(f.stencil_dists), np.float32)
+    fL = np.ascontiguousarray(np.asarray(f.L, np.float32).reshape(-1))
+    fnrm = np.ascontiguousarray(np.asarray(f.n), np.float32)
+    fno = np.asarray(f.nodes_index, np.int64)
+    t = np.asarray(n.type).reshape(-1)
+    nr = np.asarray(n.rho, np.float64).reshape(-1)
+    cen = np.ascontiguousarray(np.asarray(m.cell_centers, np.float64))
+    area = np.asarray(m.cell_areas, np.float64).reshape(-1)
+    N, F = cen.shape[0], fc.shape[0]
+    if cf.shape != (N, 3) or fc.shape != (F, 2) or fd.shape != (F, 2) or fL.shape != (F,) or fnrm.shape != (F, 2):
+        raise ValueError("the GPU features take triangles (3 face slots per cell) with per-face stencils")
+    if N and (cf.max() >= F or cf.min() < -1):
+        raise ValueError("cell face index out of range")
+    if F and (fc.max() >= N or fc.min() < -1):
+        raise ValueError("face cell index out of range")
+    inner = (fc[:, 0] >= 0) & (fc[:, 1] >= 0)
+    bnd = ~inner
+    open_ = bnd & (t[fno[:, 0]] == 2) & (t[fno[:, 1]] == 2)
+    kind = np.where(inner, 0, np.where(open_, 2, 1)).astype(np.uint8)
+    d = max(rho_in - rho_out, 1e-30)
+    phib = np.zeros(F, np.float32)
+    phib[open_] = (0.5 * ((nr[fno[open_, 0]] - rho_out) + (nr[fno[open_, 1]] - rho_out)) / d).astype(np.float32)
+    wall = np.asarray(m.face_centers, np.float64)[bnd & ~open_]
+    return {"N": N, "F": F, "cf": cf, "cs": cs, "fc": fc, "fd": fd, "fL": fL, "fn": fnrm, "kind": kind,
+            "phib": phib, "cen": cen, "area": area.astype(np.float32), "wall": wall.astype(np.float32),
+            "rho_in": rho_in, "rho_out": rho_out, "has_open": bool(open_.any())}
+
+
+def predict_cases(net, cases, rho_in, rho_out, batch_cells: int = 2_000_000, rtol: float = 1e-6,
+                  max_iter: int = 50_000):
+    """The network's predictions (target units, [N_i, 3] each) for cases
+    (dynamics, cells, faces, nodes, mesher), with every input built on the
+    GPU: the features (wall distance, the potential-flow solve of all cases
+    as one block-diagonal system, its gradient) and the aggregation stages
+    (include/fvdbm_mpnn.h ``fvdbm_ws_*``), the same quantities as ``sample``
+    builds on the host.  The network runs over groups of cases of at most
+    ``batch_cells`` cells.  Returns (predictions, pcg iterations, pcg
+    relative residual)."""
+    import ctypes as C
+
+    import torch
+    L, P = nat.lib(), MPNN._p
+    dev = torch.device(net._dev)
+    st = net._stream()
+    chk = nat.check
+    arr = [_case_arrays(cs, ri, ro) for cs, ri, ro in zip(cases, rho_in, rho_out)]
+    up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    D = []
+    for a in arr:
+        D.append({k: up(a[k]) for k in ("cf", "cs", "fc", "fd", "fL", "fn", "kind", "phib", "area")})
+        D[-1]["cen"] = up(a["cen"])
+        D[-1]["cx"] = up(a["cen"][:, 0].astype(np.float32))
+        D[-1]["cy"] = up(a["cen"][:, 1].astype(np.float32))
+        D[-1]["wx"] = up(a["wall"][:, 0].copy()) if a["wall"].shape[0] else None
+        D[-1]["wy"] = up(a["wall"][:, 1].copy()) if a["wall"].shape[0] else None
+    offs = np.concatenate([[0], np.cumsum([a["N"] for a in arr])]).astype(np.int64)
+    ntot = int(offs[-1])
+    if 4 * ntot >= 2 ** 31:
+        raise ValueError("too many cells for one feature build")
+    x = torch.empty((ntot, NFEAT), dtype=torch.float32, device=dev)
+    acol = torch.empty(4 * ntot, dtype=torch.int32, device=dev)
+    aval = torch.empty(4 * ntot, dtype=torch.float32, device=dev)
+    rhs = torch.empty(ntot, dtype=torch.float32, device=dev)
+    wd = torch.empty(ntot, dtype=torch.float32, device=dev)
+    ngx = torch.empty(ntot, dtype=torch.float32, device=dev)
+    ngy = torch.empty(ntot, dtype=torch.float32, device=dev)
+    for a, d, o in zip(arr, D, offs[:-1]):
+        n, o = a["N"], int(o)
+        chk(L.fvdbm_ws_wall_distance(n, P(d["cx"]), P(d["cy"]), a["wall"].shape[0], P(d["wx"]), P(d["wy"]),
+                                     P(wd[o:]), st))
+        chk(L.fvdbm_ws_potential_rows(n, P(d["cf"]), P(d["fc"]), P(d["fd"]), P(d["fL"]), P(d["kind"]),
+                                      P(d["phib"]), o, P(acol[4 * o:]), P(aval[4 * o:]), P(rhs[o:]), st))
+    # the potential-flow systems of every case in one solve (fvdbm_pcg)
+    ip = torch.arange(0, 4 * ntot + 1, 4, dtype=torch.int32, device=dev)
+    phi = torch.zeros(ntot, dtype=torch.float32, device=dev)
+    wb = int(L.fvdbm_pcg_work_bytes(ntot))
+    work = torch.empty(wb, dtype=torch.uint8, device=dev)
+    it, rel = C.c_int32(0), C.c_double(0.0)
+    chk(L.fvdbm_pcg(ntot, P(ip), P(acol), P(aval), P(rhs), P(phi), int(max_iter), float(rtol), 100, P(work), wb,
+                    st, C.byref(it), C.byref(rel)))
+    if not np.isfinite(rel.value):
+        raise nat.FvdbmError("fvdbm_pcg: non-finite residual")
+    del work, acol, aval, rhs, ip
+    for a, d, o in zip(arr, D, offs[:-1]):
+        n, o = a["N"], int(o)
+        chk(L.fvdbm_ws_potential_grad(n, P(d["cf"]), P(d["cs"]), P(d["fc"]), P(d["fd"]), P(d["fL"]), P(d["fn"]),
+                                      P(d["kind"]), P(d["phib"]), P(phi[o:]), P(d["area"]), P(ngx[o:]),
+                                      P(ngy[o:]), st))
+        if not a["has_open"]:  # no open boundary: the host path's zeros
+            phi[o:o + n].zero_()
+            ngx[o:o + n].zero_()
+            ngy[o:o + n].zero_()
+        x[o:o + n, 0] = d["cx"]
+        x[o:o + n, 1] = d["cy"]
+        x[o:o + n, 3] = d["area"]
+        x[o:o + n, 4] = float(np.float32(a["rho_in"]))
+        x[o:o + n, 5] = float(np.float32(a["rho_out"]))
+    x[:, 2] = wd
+    x[:, 6] = phi
+    x[:, 7] = ngx
+    x[:, 8] = ngy
+    xn = (x - torch.from_numpy(net.x_mu).to(dev)) / torch.from_numpy(net.x_sd).to(dev)
+    del x
+    # groups of cases for the network
+    groups, cur, cells = [], [], 0
+    for k, a in enumerate(arr):
+        if cur and cells + a["N"] > batch_cells:
+            groups.append(cur)
+            cur, cells = [], 0
+        cur.append(k)
+        cells += a["N"]
+    if cur:
+        groups.append(cur)
+    nmax = max(sum(arr[k]["N"] for k in g) for g in groups)
+    H = net.hidden
+    buf = {"h": [torch.empty((nmax, H), device=dev) for _ in range(net.layers + 1)],
+           "z": [torch.empty((nmax, H), device=dev) for _ in range(net.layers + 1)],
+           "m": [torch.empty((nmax, H), device=dev) for _ in range(net.layers)],
+           "y": torch.empty((nmax, NOUT), device=dev)}
+    preds = [None] * len(arr)
+    for grp in groups:
+        gofs = np.concatenate([[0], np.cumsum([arr[k]["N"] for k in grp])]).astype(np.int64)
+        ng = int(gofs[-1])
+        o0 = int(offs[grp[0]])
+        agg = []
+        for sc in net.scales:
+            if sc == "mesh":
+                col = torch.empty(3 * ng, dtype=torch.int32, device=dev)
+                wt = torch.empty(3 * ng, dtype=torch.float32, device=dev)
+                for k, go in zip(grp, gofs[:-1]):
+                    chk(L.fvdbm_ws_mesh_mean(arr[k]["N"], P(D[k]["cf"]), P(D[k]["fc"]), int(go), P(col[3 * int(go):]),
+                                             P(wt[3 * int(go):]), st))
+                ipm = torch.arange(0, 3 * ng + 1, 3, dtype=torch.int32, device=dev)
+                rows = torch.arange(0, ng + 1, dtype=torch.int32, device=dev)
+                agg.append([{"rows": ng, "cols": ng, "M": (ipm, col, wt, ipm, rows), "nchM": ng, "pM": None,
+                             "tmp": None}])
+                continue
+            counted = isinstance(sc, str) and sc.startswith("c")
+            gg = int(sc[1:]) if counted else int(sc)
+            nb = gg * gg
+            bins = torch.empty(ng, dtype=torch.int32, device=dev)
+            count = torch.zeros(nb * len(grp), dtype=torch.int32, device=dev)
+            for j, (k, go) in enumerate(zip(grp, gofs[:-1])):
+                cen = arr[k]["cen"]
+                lo, hi = cen.min(0), cen.max(0)
+                sp = np.maximum(hi - lo, 1e-30)
+                chk(L.fvdbm_ws_bin_ids(arr[k]["N"], P(D[k]["cen"]), float(lo[0]), float(lo[1]), float(sp[0]),
+                                       float(sp[1]), gg, P(bins[int(go):]), P(count[nb * j:]), st))
+            cnt = count.cpu().numpy().astype(np.int64)
+            ipp = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
+            wbin = np.empty(nb * len(grp), np.float32)
+            for j, k in enumerate(grp):
+                c_ = cnt[nb * j:nb * (j + 1)]
+                wbin[nb * j:nb * (j + 1)] = (np.full(nb, nb / arr[k]["N"]) if counted
+                                             else 1.0 / np.maximum(c_, 1)).astype(np.float32)
+            t_ip, t_w = up(ipp), up(wbin)
+            pcol = torch.empty(ng, dtype=torch.int32, device=dev)
+            pwt = torch.empty(ng, dtype=torch.float32, device=dev)
+            ucol = torch.empty(ng, dtype=torch.int32, device=dev)
+            for j, (k, go) in enumerate(zip(grp, gofs[:-1])):
+                chk(L.fvdbm_ws_bin_rows(arr[k]["N"], nb, P(bins[int(go):]), P(t_ip[nb * j:]), P(t_w[nb * j:]),
+                                        int(go), nb * j, P(pcol), P(pwt), P(ucol[int(go):]), st))
+            cs_, cp_ = _chunks(ipp)
+            nch = int(cp_[-1])
+            rows_b = nb * len(grp)
+            ipu = torch.arange(0, ng + 1, dtype=torch.int32, device=dev)
+            ones = torch.ones(ng, dtype=torch.float32, device=dev)
+            agg.append([{"rows": rows_b, "cols": ng, "M": (t_ip, pcol, pwt, up(cs_), up(cp_)), "nchM": nch,
+                         "pM": torch.empty((nch, H), device=dev) if nch > rows_b else None,
+                         "tmp": torch.empty((rows_b, H), device=dev)},
+                        {"rows": ng, "cols": rows_b, "M": (ipu, ucol, ones, ipu, ipu), "nchM": ng, "pM": None,
+                         "tmp": None}])
+        g = {"n": ng, "x": xn[o0:o0 + ng], "agg": agg, "h": [a_[:ng] for a_ in buf["h"]],
+             "z": [a_[:ng] for a_ in buf["z"]], "m": [a_[:ng] for a_ in buf["m"]], "y": buf["y"][:ng]}
+        net._forward(g)
+        y = g["y"].detach().cpu().numpy() * net.t_sd + net.t_mu
+        for k, a0, a1 in zip(grp, gofs[:-1], gofs[1:]):
+            preds[k] = y[int(a0):int(a1)]
+    return preds, int(it.value), float(rel.value)
 
 
 def macros(pdf):

@@ -83,14 +83,49 @@ int fvdbm_mp_to_bf16(const float *x, uint16_t *y, size_t count, void *stream);
  * Laplacian per case, many cases as one block-diagonal system).  x holds the
  * initial guess on entry and the solution on return.  Iterates until
  * ||r|| <= rtol ||b|| (tested every check_every iterations, where the call
- * synchronises the stream) or max_iter.  Dot products are summed in double
- * in a fixed order: bitwise reproducible.  work: device scratch of at least
+ * synchronises the stream) or max_iter.  Dot products are summed per thread
+ * in float32, then in double over blocks, in a fixed order: bitwise
+ * reproducible.  work: device scratch of at least
  * fvdbm_pcg_work_bytes(n) bytes.  *iters and *rel_res report the end state
  * (rel_res NaN: A was not positive definite or the input not finite). */
 size_t fvdbm_pcg_work_bytes(int32_t n);
 int fvdbm_pcg(int32_t n, const int32_t *indptr, const int32_t *indices, const float *values, const float *b,
               float *x, int32_t max_iter, double rtol, int32_t check_every, void *work, size_t work_bytes,
               void *stream, int32_t *iters, double *rel_res);
+
+/* Features built on the GPU, one case per call (the host path of
+ * fvdbm-jax_gb300/warmstart.py computes the same quantities).  Cell and face
+ * indices are the case's own; col_off / cell_off / bin_off shift the column
+ * indices a case writes, so that several cases form one block-diagonal
+ * matrix.  face_kind: 0 interior, 1 wall, 2 open (both end nodes density
+ * nodes); face_phib: the potential on open faces. */
+/* Distance from each cell centre to the nearest of n_wall wall points. */
+int fvdbm_ws_wall_distance(int32_t n, const float *cx, const float *cy, int32_t n_wall, const float *wx,
+                           const float *wy, float *out, void *stream);
+/* The potential-flow system in rows of four entries (diagonal, then the three
+ * face slots; zero entries on the diagonal's column where a slot has no
+ * interior neighbour): col [4n], val [4n], rhs [n]. */
+int fvdbm_ws_potential_rows(int32_t n, const int32_t *cell_faces, const int32_t *face_cells,
+                            const float *face_dists, const float *face_L, const uint8_t *face_kind,
+                            const float *face_phib, int32_t col_off, int32_t *col, float *val, float *rhs,
+                            void *stream);
+/* -grad phi per cell (Green-Gauss over the face values). */
+int fvdbm_ws_potential_grad(int32_t n, const int32_t *cell_faces, const float *cell_signs,
+                            const int32_t *face_cells, const float *face_dists, const float *face_L,
+                            const float *face_n, const uint8_t *face_kind, const float *face_phib,
+                            const float *phi, const float *area, float *ngx, float *ngy, void *stream);
+/* Mesh-mean stage in rows of three entries: the interior neighbours in
+ * ascending order with weight 1/degree, then zero weights on the own cell. */
+int fvdbm_ws_mesh_mean(int32_t n, const int32_t *cell_faces, const int32_t *face_cells, int32_t col_off,
+                       int32_t *col, float *wt, void *stream);
+/* Bin of each cell on a g x g grid over [lo, lo + span] (double), and the
+ * bins' populations added into count [g*g]. */
+int fvdbm_ws_bin_ids(int32_t n, const double *cell_xy, double lo_x, double lo_y, double span_x, double span_y,
+                     int32_t g, int32_t *bin, int32_t *count, void *stream);
+/* The bin stage's rows (cells of each bin in ascending order, weight
+ * wbin[bin], from start[bin]) and each cell's bin column (ucol). */
+int fvdbm_ws_bin_rows(int32_t n, int32_t n_bins, const int32_t *bin, const int32_t *start, const float *wbin,
+                      int32_t cell_off, int32_t bin_off, int32_t *pcol, float *pwt, int32_t *ucol, void *stream);
 
 #ifdef __cplusplus
 }

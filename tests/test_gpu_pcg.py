@@ -61,3 +61,28 @@ def test_predict_many_equals_predict():
         assert len(many) == len(one)
         for a, b in zip(one, many):
             assert np.array_equal(a, b)
+
+
+def test_predict_cases_on_the_gpu_matches_the_host_path():
+    """Features and stages built on the GPU (warmstart.predict_cases) give the
+    network the same inputs as the host path (sample + solve_potentials +
+    predict_many): the same predictions up to the potential solve's rounding,
+    and the same bits on a repeat."""
+    from fvdbm_jax_gb300 import warmstart as WS
+    cs = _cases()
+    smp = [WS.sample(case, rin, rout, defer_potential=True) for case, rin, rout in cs]
+    WS.solve_potentials(smp, rtol=1e-6)
+    net = WS.MPNN(seed=5)
+    x = np.concatenate([s.x for s in smp])
+    net.x_mu, net.x_sd = x.mean(0), np.maximum(x.std(0), 1e-12)
+    host = net.predict_many(smp)
+    rin, rout = [c[1] for c in cs], [c[2] for c in cs]
+    for bc in (10 ** 9, 20_000):
+        gpu, it, rel = WS.predict_cases(net, [c[0] for c in cs], rin, rout, batch_cells=bc)
+        again, _, _ = WS.predict_cases(net, [c[0] for c in cs], rin, rout, batch_cells=bc)
+        assert rel <= 1e-6 and it > 0
+        for h, g, g2 in zip(host, gpu, again):
+            assert np.array_equal(g, g2)
+            assert g.shape == h.shape
+            scale = np.abs(h).max(0)
+            assert np.all(np.abs(g - h).max(0) <= 1e-3 * scale + 1e-6), (np.abs(g - h).max(0), scale)
