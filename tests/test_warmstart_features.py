@@ -96,3 +96,37 @@ def test_potential_system_and_deferred_sample():
     assert not s.x[:, 6:].any()
     full = WS.sample((dyn, c, f, n, m), 1.02, 0.98)
     assert full.pending is None and np.array_equal(full.x[:, :6], s.x[:, :6])
+
+
+def test_gpu_feature_inputs_match_the_host_system():
+    """The host side of the GPU feature path (warmstart._case_arrays): face
+    kinds and open-face potentials as the host potential system uses them,
+    wall points as the host wall distance uses them, and index ranges
+    checked before anything reaches a kernel."""
+    import copy
+    import pytest
+    from fvdbm_jax_gb300 import cases
+    from fvdbm_jax_gb300 import warmstart as WS
+    case = cases.porous_square(10, 2500, 0.65, rho_in=1.02, rho_out=0.98, porosity=0.8, delta_t=1.0, seed=9,
+                               mesher=True)
+    dyn, c, f, n, m = case
+    a = WS._case_arrays(case, 1.02, 0.98)
+    fc = np.asarray(f.stencil_cells_index)
+    assert np.array_equal(a["kind"] == 0, (fc[:, 0] >= 0) & (fc[:, 1] >= 0))
+    ps = WS.potential_system(m, c, f, n, 1.02, 0.98)
+    # rhs of the host system from the kinds and boundary values
+    sd = np.asarray(f.stencil_dists, np.float64)
+    L = np.asarray(f.L, np.float64).reshape(-1)
+    op = a["kind"] == 2
+    owner = np.where(fc[:, 0] >= 0, fc[:, 0], fc[:, 1])
+    rhs = np.bincount(owner[op], L[op] / sd[op, 0] * a["phib"][op].astype(np.float64), a["N"])
+    assert np.allclose(rhs, ps.rhs, rtol=1e-6, atol=1e-12)
+    from scipy.spatial import cKDTree
+    wd = cKDTree(a["wall"].astype(np.float64)).query(a["cen"])[0]
+    assert np.allclose(wd, WS.wall_distance(m, f, n), rtol=1e-6, atol=1e-6)
+    bad = copy.deepcopy(case)
+    fi = np.array(bad[1].face_indices)
+    fi[0, 0] = a["F"] + 5
+    bad[1].face_indices = fi
+    with pytest.raises(ValueError, match="out of range"):
+        WS._case_arrays(bad, 1.02, 0.98)
