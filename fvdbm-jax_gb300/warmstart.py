@@ -757,6 +757,10 @@ def predict_cases(net, cases, rho_in, rho_out, batch_cells: int = 2_000_000, rto
     import ctypes as C
 
     import torch
+    if len(cases) != len(rho_in) or len(cases) != len(rho_out):
+        raise ValueError("one inlet and one outlet density per case")
+    if not cases:
+        return [], 0, 0.0
     L, P = nat.lib(), MPNN._p
     dev = torch.device(net._dev)
     st = net._stream()
